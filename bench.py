@@ -1,0 +1,362 @@
+"""Benchmark: HMC trajectories/s on the single-lattice 1024x1024 plain-FP64 workload.
+
+Workload (one "step" = one HMC trajectory of the hot path):
+  1024 x 1024 lattice, antiperiodic t / periodic x, m = 0.05, g = 0.6, mu = 0,
+  A_mu ~ N(0, 0.3^2) from a fixed seed, one pseudofermion phi = M^dag eta,
+  20 leapfrog steps of tau = 1, CG on M^dag M to relative residual 1e-10,
+  FP64 arithmetic (the reference's), random fields from the device Philox
+  stream.  The stochastic Re <n, M^dag n> term of hmc.c is kept (it costs one
+  operator apply per trajectory end and adds nothing at mu = 0).
+
+Output: one JSON line (rank 0).  `value` is device-timed trajectories/s with the
+gauge field resident in HBM; `e2e` the same through the public C ABI with the
+gauge field uploaded from and downloaded to host memory every trajectory.
+`roofline` is the CG iteration (k_cg1 + k_cg2_64 + k_cg3, >90% of the device
+time), timed with CUDA events inside the trajectory graph, against the
+algorithmic 208 B/site of one FP64 CG iteration.  Also reported: the operator
+apply alone (20 M and 20 M^dag applies, 64 B/site) and the same trajectories
+with the mixed-precision solver (FP32 CG + FP64 reliable updates every 50
+iterations) started from the same field and random stream.
+
+`--impl reference` times the reference hmc.c (adjoint-corrected build in
+oracle/_ref, single-threaded as the reference is) on a bounded sample: 20
+iterations of its fmdm_invert_cg at 1024^2 per step, scaled to a trajectory
+by the CG iteration count of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+W = dict(nt=1024, nx=1024, m=0.05, g=0.6, mu=0.0, bc_t=-1, bc_x=1, sigma=0.3, nsteps=20, tau=1.0, rel_tol=1e-10,
+         npf=1, seed=20241203)
+WORKLOAD_NAME = "1024x1024 plain-FP64 HMC trajectory (20 leapfrog steps, tau 1, CG rel 1e-10, m 0.05, g 0.6)"
+# Algorithmic bytes per site: one FP64 CG iteration (M^dag M 64 + x,r update 96 + p update 48)
+CG_ITER_BYTES_PER_SITE = 208
+DSLASH_BYTES_PER_SITE = 64
+# CG iterations per trajectory of this workload (FP64 solver; sum over the 21
+# solves), measured by the GPU arm on GB300 and used to scale the reference's
+# per-iteration CPU time to a trajectory.
+CG_ITERS_PER_TRAJ = 8600
+L2_FLUSH_BYTES = 256 << 20
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_iter():
+    """DRAM bytes per CG iteration from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "cg_iteration_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, v: float) -> float:
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU reference timing (bounded sample)
+# ---------------------------------------------------------------------------
+def cpu_sample(repeats: int = 3):
+    """Seconds per CG iteration and per operator apply of the reference hmc.c at
+    1024^2 (oracle/_ref sample build: fmdm_invert_cg stops after 20 iterations),
+    or of the oracle restatement where the reference build is absent."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(W["seed"])
+    A = rng.normal(0, W["sigma"], (W["nt"], W["nx"], 2))
+    b = rng.normal(size=(W["nt"], W["nx"])) + 1j * rng.normal(size=(W["nt"], W["nx"]))
+    iters = 20
+    if O.ref_available(W["nt"], W["nx"], "sample_px"):
+        ref = O.RefHMC(W["nt"], W["nx"], W["m"], W["g"], W["mu"], warmup=0, variant="sample_px")
+        ref.set_A(A)
+        kind = "reference"
+        t0 = time.perf_counter()
+        ref.M(b)
+        t_apply = time.perf_counter() - t0
+        ts = []
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            ref.cg(b)
+            ts.append(time.perf_counter() - t0)
+    else:
+        o = O.Oracle(W["nt"], W["nx"], W["m"], W["g"], W["mu"], W["bc_t"], W["bc_x"])
+        kind = "port"
+        t0 = time.perf_counter()
+        o.M(A, b)
+        t_apply = time.perf_counter() - t0
+        ts = []
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            o.cg(A, b, rel_tol=0, abs_tol2=0, maxiter=iters)
+            ts.append(time.perf_counter() - t0)
+    t_iter = min(ts) / iters
+    # per trajectory: CG iterations + the non-CG applies (phi = M^dag eta, M chi per
+    # MD step, two stochastic-term applies)
+    t_traj = t_iter * CG_ITERS_PER_TRAJ + t_apply * (W["nsteps"] + 3)
+    sample = (f"{repeats} x {iters} iterations of fmdm_invert_cg + 1 fm_mul at {W['nt']}x{W['nx']} "
+              f"({'reference hmc.c build' if kind == 'reference' else 'oracle restatement'}), "
+              f"scaled by {CG_ITERS_PER_TRAJ} CG iterations and {W['nsteps'] + 3} applies per trajectory")
+    return dict(value=1.0 / t_traj, unit="trajectories/s", cores=1, kind=kind, sample=sample,
+                sec_per_cg_iter=t_iter, sec_per_apply=t_apply)
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    vals = []
+    cs = None
+    for i in range(args.warmup + args.steps):
+        cs = cpu_sample(repeats=1)
+        if i >= args.warmup:
+            vals.append(cs["value"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": "HMC trajectories/s (1024^2 plain FP64)", "value": v,
+            "unit": "trajectories/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": config_block(),
+            "cpu_baseline": {k: cs[k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": "trajectories/s"},
+            "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def config_block():
+    return {"workload": WORKLOAD_NAME, "lattice": f"{W['nt']}x{W['nx']}", "m": W["m"], "g": W["g"], "mu": W["mu"],
+            "bc": "t antiperiodic, x periodic", "A_sigma": W["sigma"], "nsteps": W["nsteps"], "tau": W["tau"],
+            "cg_rel_tol": W["rel_tol"], "pseudofermions": W["npf"], "rng": "Philox4x32-10 on device",
+            "l2": "256 MiB buffer written between timed trajectories", "parallelism": "replicas"}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_ours(args, ws, rank, local):
+    import torch
+
+    import thirring2d_gb300 as tg
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nt, nx = W["nt"], W["nx"]
+    V = nt * nx
+    rng = np.random.default_rng(W["seed"] + rank)
+    A0 = rng.normal(0, W["sigma"], (nt, nx, 2))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def make(precision):
+        L = tg.Lattice(nt, nx, W["m"], W["g"], W["mu"], W["bc_t"], W["bc_x"], device=local)
+        L.set_gauge(A0)
+        cg = tg.cg_params(rel_tol=W["rel_tol"], abs_tol2=0.0, precision=precision, ru_interval=50)
+        hp = tg.hmc_params(nsteps=W["nsteps"], tau=W["tau"], npf=W["npf"], stochastic_term=True,
+                           rng=tg.native.RNG_PHILOX, seed=W["seed"] + rank, use_graph=True, cg=cg)
+        return L, hp
+
+    def timed_loop(L, hp, steps, warmup):
+        stream = torch.cuda.ExternalStream(L.lib.tg_stream(L.h), device=dev)
+        for _ in range(warmup):
+            r = L.update_gauge(hp)
+            assert r.status == 0, r.as_dict()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        res = []
+        barrier(ws)
+        torch.cuda.synchronize()
+        with Clocks(local) as clk:
+            for i in range(steps):
+                with torch.cuda.stream(stream):
+                    flush.fill_(float(i))
+                evs[i][0].record(stream)
+                r = L.update_gauge(hp)
+                evs[i][1].record(stream)
+                res.append(r)
+            torch.cuda.synchronize()
+        barrier(ws)
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        return ms, res, clk.summary()
+
+    # ---- plain FP64 (the headline) ----
+    L64, hp64 = make(tg.native.PREC_FP64)
+    ms, res, clocks = timed_loop(L64, hp64, args.steps, args.warmup)
+    ms_max = allmax(ws, ms)
+    value = ws * args.steps / (ms_max / 1000.0)
+    iters = sum(r.cg_iterations for r in res)
+    cg_ms = sum(r.cg_ms for r in res)
+    for r in res:
+        assert r.status == 0, r.as_dict()
+
+    # ---- e2e through the public API with host buffers ----
+    A_host = L64.get_gauge()
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        L64.set_gauge(A_host)                    # H2D: 16 B/site
+        r = L64.update_gauge(hp64)
+        A_host = L64.get_gauge()                 # D2H: 16 B/site + the result struct
+    t_e2e = allmax(ws, time.perf_counter() - t0)
+    e2e_value = ws * args.steps / t_e2e
+
+    # ---- operator alone: 20 M and 20 M^dag applies (64 B/site) ----
+    t_M = L64.time_apply(20, False, tg.native.PREC_FP64)
+    t_Md = L64.time_apply(20, True, tg.native.PREC_FP64)
+    dslash_gbs = DSLASH_BYTES_PER_SITE * V / (0.5 * (t_M + t_Md) * 1e-3) / 1e9
+    t_M32 = L64.time_apply(20, False, tg.native.PREC_MIXED)
+    dslash32_gbs = 32 * V / (t_M32 * 1e-3) / 1e9
+
+    # ---- mixed precision on the same field and random stream ----
+    Lmx, hpmx = make(tg.native.PREC_MIXED)
+    Lref, _ = make(tg.native.PREC_FP64)
+    mx_pairs = []
+    for _ in range(2):                          # same start, same Philox stream: dH agreement
+        a = Lref.update_gauge(hp64)
+        b = Lmx.update_gauge(hpmx)
+        mx_pairs.append((a.dH, b.dH, a.accepted, b.accepted))
+    Lmx.set_gauge(A0)
+    ms_mx, res_mx, _ = timed_loop(Lmx, hpmx, args.steps, max(0, args.warmup - 2))
+    ms_mx = allmax(ws, ms_mx)
+    mixed_value = ws * args.steps / (ms_mx / 1000.0)
+
+    hbm, peak_kind = peaks()
+    t_iter_ms = cg_ms / max(1, iters)
+    achieved = CG_ITER_BYTES_PER_SITE * V / (t_iter_ms * 1e-3) / 1e9
+    traf = traffic_per_iter()
+    launches = sum(1 + 3 * r.cg_iterations for r in res) + args.steps * (3 * W["nsteps"] + 20)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": "HMC trajectories/s (1024^2 plain FP64) + Dslash HBM GB/s",
+        "value": value, "unit": "trajectories/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Gaussian A_mu, Philox pseudofermion/momentum fields)",
+        "config": config_block(),
+        "e2e": {"value": e2e_value, "unit": "trajectories/s", "h2d_bytes_per_step": 16 * V,
+                "d2h_bytes_per_step": 16 * V + 128},
+        "roofline": {"kernel": "CG iteration (k_cg1 + k_cg2_64 + k_cg3), FP64", "bound": "hbm",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": peak_kind, "bytes_per_site": CG_ITER_BYTES_PER_SITE,
+                     "ms_per_iteration": t_iter_ms,
+                     "traffic": (traf["bytes_per_site"] * V if traf else None)},
+        "dslash": {"fp64_gbs": dslash_gbs, "fp64_ms_M": t_M, "fp64_ms_Mdag": t_Md, "fp64_frac": dslash_gbs / hbm,
+                   "fp32_gbs": dslash32_gbs, "fp32_ms": t_M32, "bytes_per_site_fp64": 64, "bytes_per_site_fp32": 32},
+        "mixed": {"value": mixed_value, "unit": "trajectories/s", "speedup_vs_fp64": mixed_value / value,
+                  "cg_iterations_per_traj": statistics.mean(r.cg_iterations for r in res_mx),
+                  "reliable_updates_per_traj": statistics.mean(r.reliable_updates for r in res_mx),
+                  "dH_pairs_fp64_vs_mixed": mx_pairs},
+        "cg_iterations_per_traj": iters / args.steps,
+        "dH": [r.dH for r in res], "accepted": [r.accepted for r in res],
+        "clocks": clocks, "gpu_launches": launches,
+    }
+    if ws == 1:
+        cs = cpu_sample()
+        line["cpu_baseline"] = {k: cs[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

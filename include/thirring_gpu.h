@@ -1,0 +1,183 @@
+/*
+ * thirring_gpu.h -- C ABI of the GB300 (sm_103a) Thirring2D HMC library.
+ *
+ * One tg_lattice holds one lattice (NT x NX sites), its couplings, its
+ * device-resident fields and a CUDA stream.  All entry points take plain
+ * pointers and sizes; "host" buffers are ordinary CPU memory, "_dev" buffers
+ * are device pointers on the lattice's device.  Every call returns a status
+ * (TG_OK = 0); tg_last_error() gives the message of the last failure on the
+ * calling thread.  Nothing here calls exit().  Calls that run CG return the
+ * solver's status (TG_E_NOCONV, TG_E_DIVERGED, TG_E_NAN) when a solve did not
+ * converge; their outputs and result structs are still written.
+ *
+ * Field layouts (identical to the reference's row-pointer arrays flattened
+ * t-major, hmc.c:105-112 and 888-898):
+ *   gauge field / momenta / forces   double[NT*NX*2]   index (t*NX + x)*2 + dir
+ *   fermion vectors                  double[NT*NX*2]   interleaved (re, im) of
+ *                                                      complex v[t][x]
+ *
+ * The reference (rantahar/Thirring2D) has no library; its interface is the
+ * function set of hmc.c.  Each entry point below names the function it
+ * replaces.  include/thirring_hmc.h declares the drop-in with the
+ * reference's exact names and signatures, built on top of this API.
+ */
+#ifndef THIRRING_GPU_H
+#define THIRRING_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define TG_OK 0
+#define TG_E_NOCONV 1   /* CG reached maxiter (hmc.c:364 stops silently)                      */
+#define TG_E_DIVERGED 2 /* |r|^2/|r0|^2 > 1e10 (hmc.c:383-386: "Cannot invert fermion matrix") */
+#define TG_E_NAN 3      /* NaN in a CG recurrence                                             */
+#define TG_E_CUDA 4     /* CUDA runtime error                                                 */
+#define TG_E_ARG 5      /* invalid argument                                                   */
+#define TG_E_ALLOC 6    /* device or pinned allocation failed                                 */
+
+/* ---- boundary conditions (sign of the hop across the last slice) ------- */
+#define TG_BC_PERIODIC 1
+#define TG_BC_ANTIPERIODIC (-1) /* hmc.c:143-148 (t) and 165-180 (x) as shipped */
+#define TG_BC_OPEN 0
+
+/* ---- solver precision --------------------------------------------------- */
+#define TG_PREC_FP64 0  /* all of CG in FP64, the reference's arithmetic          */
+#define TG_PREC_MIXED 1 /* FP32 CG with FP64 reliable updates of x and b - A x    */
+
+/* ---- random numbers of a trajectory --------------------------------------- */
+#define TG_RNG_MT 0       /* the reference's MT19937 stream (mersenne.h), drawn on the host */
+#define TG_RNG_PHILOX 1   /* Philox4x32-10 on the device, keyed by seed and trajectory      */
+#define TG_RNG_EXTERNAL 2 /* caller supplies the Gaussian fields (tg_trajectory_ext)        */
+
+typedef struct tg_lattice tg_lattice;
+
+typedef struct {
+  int nt, nx;       /* NT, NX (hmc.c:14-15, compile-time constants there)  */
+  double m, g, mu;  /* mass, coupling, chemical potential (hmc.c:38-40)    */
+  int bc_t, bc_x;   /* TG_BC_*; the reference ships ANTIPERIODIC for both  */
+  int device;       /* CUDA device ordinal                                  */
+} tg_lattice_params;
+
+typedef struct {
+  double rel_tol;   /* stop when |r| < rel_tol |b| (0 disables)                      */
+  double abs_tol2;  /* stop when |r|^2 < abs_tol2 (hmc.c:34 CG_ACCURACY = 1e-30)     */
+  int maxiter;      /* iteration cap (hmc.c:35 CG_MAX_ITER = 100000)                  */
+  int precision;    /* TG_PREC_*                                                      */
+  int ru_interval;  /* TG_PREC_MIXED: FP32 iterations between FP64 reliable updates   */
+  int pad_;
+} tg_cg_params;
+
+typedef struct {
+  int iterations;       /* CG iterations (each = one M and one M^dagger apply) */
+  int status;           /* TG_OK, TG_E_NOCONV, TG_E_DIVERGED or TG_E_NAN        */
+  int reliable_updates; /* TG_PREC_MIXED only                                   */
+  int pad_;
+  double rr;            /* final |r|^2 (true residual after a reliable update)  */
+  double rr0;           /* |b|^2                                                */
+} tg_cg_result;
+
+typedef struct {
+  int nsteps;              /* leapfrog steps (hmc.c:708 uses 10)                          */
+  double tau;              /* trajectory length (hmc.c:709 uses 1)                         */
+  int npf;                 /* pseudofermions (hmc.c uses 1; at most 8)                     */
+  int stochastic_term;     /* 1: include Re <n, M^dag n> and its force (hmc.c:467-479,
+                              608-661, 698-699) -- it consumes V Gaussian pairs per
+                              trajectory and vanishes identically at mu = 0              */
+  int rng;                 /* TG_RNG_MT or TG_RNG_PHILOX for tg_trajectory                 */
+  int use_graph;           /* 1: run the trajectory as one CUDA graph (CG loops as
+                              conditional WHILE nodes); 0: eager launches              */
+  unsigned long long seed; /* Philox key                                                  */
+  tg_cg_params cg;         /* solver used inside the trajectory                           */
+} tg_hmc_params;
+
+typedef struct {
+  double dH;                         /* H_end - H_start, hmc.c:729-732 order  */
+  double Sg0, Spf0, Smd0, Smom0;     /* actions at the start (hmc.c:695-699)  */
+  double Sg1, Spf1, Smd1, Smom1;     /* actions at the end (hmc.c:719-726)    */
+  double u_accept;                   /* the uniform compared with exp(-dH)    */
+  int accepted;                      /* exp(-dH) > u  (hmc.c:738)             */
+  int status;                        /* worst CG status of the trajectory     */
+  int cg_solves, cg_iterations;      /* totals over the trajectory            */
+  int cg_max_iterations, reliable_updates;
+  double cg_ms;                      /* device time inside CG solves          */
+} tg_traj_result;
+
+/* ---- context ------------------------------------------------------------ */
+const char* tg_last_error(void);
+const char* tg_version(void);
+/* Allocates every device field of the lattice (about 40 x 16 B x NT*NX).
+ * A starts at 0, as hmc.c:896. */
+int tg_create(const tg_lattice_params* p, tg_lattice** out);
+int tg_destroy(tg_lattice* L);
+/* m, g, mu are globals the reference reads at every call (hmc.c:38-40). */
+int tg_set_couplings(tg_lattice* L, double m, double g, double mu);
+int tg_get_params(const tg_lattice* L, tg_lattice_params* p);
+int tg_synchronize(tg_lattice* L);
+void* tg_stream(tg_lattice* L); /* the lattice's cudaStream_t */
+
+/* ---- gauge field: the reference's global double ***A (hmc.c:47) --------- */
+int tg_set_gauge(tg_lattice* L, const double* A);
+int tg_get_gauge(tg_lattice* L, double* A);
+int tg_set_gauge_dev(tg_lattice* L, const void* A_dev);
+
+/* ---- operator ---------------------------------------------------------- */
+/* fm_mul (hmc.c:123-184): out = M in.  dagger = 1: fm_conjugate_mul
+ * (hmc.c:188-249) as the true adjoint M^dagger = m - D(-mu).  The shipped
+ * fm_conjugate_mul is a verbatim copy of fm_mul, which makes the reference's
+ * CG diverge; this library applies the adjoint.  Host buffers, FP64. */
+int tg_apply(tg_lattice* L, const double* in, double* out, int dagger);
+/* Same on device vectors: double2[V] for TG_PREC_FP64, float2[V] for
+ * TG_PREC_MIXED (the FP32 operator).  Enqueued on the lattice's stream. */
+int tg_apply_dev(tg_lattice* L, const void* in, void* out, int dagger, int precision);
+/* Times n back-to-back applies on device vectors with CUDA events on the
+ * lattice's stream; *ms_per_apply = average per launch. */
+int tg_time_apply(tg_lattice* L, int n, int dagger, int precision, double* ms_per_apply);
+
+/* ---- CG on M^dagger M: fmdm_invert_cg (hmc.c:341-404) -------------------- */
+int tg_cg(tg_lattice* L, const tg_cg_params* cp, const double* b, double* x, tg_cg_result* res);
+int tg_cg_dev(tg_lattice* L, const tg_cg_params* cp, const void* b_dev, void* x_dev, tg_cg_result* res);
+
+/* ---- actions and forces ------------------------------------------------- */
+/* calc_gauge_action (hmc.c:73-79) of the lattice's gauge field. */
+int tg_gauge_action(tg_lattice* L, double* S);
+/* pseudofermion_action (hmc.c:451-463): Re <phi, (M^dag M)^-1 phi>. */
+int tg_pseudofermion_action(tg_lattice* L, const tg_cg_params* cp, const double* phi, double* S,
+                            tg_cg_result* res);
+/* stochastic_md_action (hmc.c:467-479): Re <n, M^dag n>. */
+int tg_md_action(tg_lattice* L, const double* n, double* S);
+/* dS/dA on every link (gauge + pseudofermion + stochastic term), the force
+ * momentum_step (hmc.c:504-661) subtracts, from npf solved vectors
+ * chi_k = (M^dag M)^-1 phi_k (double[npf*V*2]); noise may be NULL. */
+int tg_force(tg_lattice* L, int npf, const double* chi, const double* noise, double* F);
+/* momentum_step (hmc.c:504-665): mom -= eps * dS/dA, solving for every
+ * pseudofermion; res (may be NULL) receives the summed CG counts. */
+int tg_momentum_step(tg_lattice* L, const tg_cg_params* cp, double* mom, int npf, const double* phi,
+                     const double* noise, double eps, tg_cg_result* res);
+/* gauge_step (hmc.c:97-101): A += 2 eps mom. */
+int tg_gauge_step(tg_lattice* L, const double* mom, double eps);
+
+/* ---- random numbers: the reference stream (mersenne_inline.c) ------------ */
+/* seed_mersenne(seed) then `warmup` discarded draws (hmc.c:874-877 uses 543210). */
+int tg_mt_seed(tg_lattice* L, long seed, long warmup);
+int tg_mt_uniforms(tg_lattice* L, double* out, long n);
+/* update_puregauge_hb (hmc.c:82-93) x sweeps, drawing from the MT stream. */
+int tg_puregauge_sweeps(tg_lattice* L, int sweeps);
+
+/* ---- HMC trajectory: update_gauge (hmc.c:671-746) ------------------------- */
+/* Draws the pseudofermion, momentum, noise fields and the accept uniform
+ * from the stream p->rng selects (TG_RNG_MT: the reference's order, so the
+ * trajectory reproduces hmc.c's on the same seed), runs the leapfrog on the
+ * device, accepts or rejects, and leaves the new A on the device. */
+int tg_trajectory(tg_lattice* L, const tg_hmc_params* p, tg_traj_result* r);
+/* Same with caller-supplied fields: eta double[npf*V*2] (phi_k = M^dag eta_k),
+ * mom double[V*2], noise double[V*2] (ignored unless stochastic_term),
+ * u_accept the uniform of hmc.c:738. */
+int tg_trajectory_ext(tg_lattice* L, const tg_hmc_params* p, const double* eta, const double* mom,
+                      const double* noise, double u_accept, tg_traj_result* r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* THIRRING_GPU_H */

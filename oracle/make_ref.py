@@ -1,0 +1,178 @@
+"""Recipe: build the reference hmc.c, with its adjoint corrected, into oracle/_ref/.
+
+TEST INFRASTRUCTURE ONLY (the oracle side of the parity tests and the
+reference arm of bench.py).  Nothing in the product imports this.
+
+The reference (rantahar/Thirring2D) has no library form: hmc.c fixes NT/NX with
+unconditional #defines (hmc.c:14-15), defines main() (hmc.c:847) and needs
+<lapacke.h> for a determinant that main never calls (hmc.c:6, 314-336).  Its
+fm_conjugate_mul (hmc.c:188-249) is a verbatim copy of fm_mul, so its CG on
+"M^dagger M" diverges and calls exit(1) (hmc.c:383-386) on every lattice tried.
+
+This script writes ONE generated source, oracle/_ref/src/hmc_patched.c, from the
+reference's own hmc.c with these textual edits and nothing else:
+
+  * ``#define NT 32`` / ``#define NX 32``  ->  ``#define NT REF_NT`` / ``REF_NX``
+    (sizes chosen per build with -D);
+  * ``int main(void)`` -> ``int hmc_reference_main(void)`` (the driver has its own
+    set-up and never calls it);
+  * ``#define CG_MAX_ITER 100000`` -> ``REF_CG_MAX_ITER`` (100000 in every build
+    except the "sample" variant, whose CG stops silently after 20 iterations as
+    hmc.c:364 does at its cap -- the bounded CPU-baseline sample of bench.py);
+  * inside fm_conjugate_mul only: every ``v += `` / ``v -= `` of a hop term is
+    multiplied by ``REF_ADJ_SIGN`` and ``exp(mu)``/``exp(-mu)`` by
+    ``REF_ADJ_MUSIGN``.  With -DREF_ADJ_SIGN=-1 -DREF_ADJ_MUSIGN=-1 the function
+    applies the true adjoint M^dagger = m - D(-mu) ("REF-FIXED"); with +1/+1 it is
+    the shipped code ("REF-EXACT");
+  * every ``x2 > x`` test (the x-boundary branches of fm_mul, fm_conjugate_mul,
+    fermion_matrix and momentum_step) becomes ``(x2 > x || REF_PERIODIC_X)``
+    after ``x2 = xup[x]`` and ``(x2 > x && !REF_PERIODIC_X)`` after
+    ``x2 = xdn[x]``, so -DREF_PERIODIC_X=1 gives a periodic x direction and 0
+    the shipped antiperiodic one.
+
+Each edit asserts how many places it changed, so a different hmc.c fails loudly.
+mersenne_inline.c / mersenne.h are copied unchanged.  oracle/ref_driver.c (own
+code) #includes the generated file and exposes flat-array entry points; one
+shared library is built per (NT, NX, variant) into oracle/_ref/.
+
+/root/reference is read only here, at generation time.  The generated sources
+stay in oracle/_ref/src (git-ignored); where the reference tree is absent (the
+GPU host) the libraries are rebuilt from those generated sources if present.
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = "/root/reference"
+OUT = os.path.join(HERE, "_ref")
+SRC = os.path.join(OUT, "src")
+
+# (nt, nx) sizes the tests, fixtures and the CPU baseline use.
+DEFAULT_SIZES = [(4, 4), (6, 4), (8, 8), (16, 16), (64, 64), (1024, 1024), (2048, 2048)]
+# sizes that also get the bounded-CG "sample" build used for CPU timing
+SAMPLE_SIZES = [(16, 16), (64, 64), (1024, 1024), (2048, 2048)]
+# variant name -> compile definitions
+VARIANTS = {
+    "fixed_apx": dict(REF_ADJ_SIGN=-1, REF_ADJ_MUSIGN=-1, REF_PERIODIC_X=0),  # reference BCs, true adjoint
+    "fixed_px": dict(REF_ADJ_SIGN=-1, REF_ADJ_MUSIGN=-1, REF_PERIODIC_X=1),   # periodic x, true adjoint
+    "exact_apx": dict(REF_ADJ_SIGN=1, REF_ADJ_MUSIGN=1, REF_PERIODIC_X=0),    # as shipped
+    "sample_px": dict(REF_ADJ_SIGN=-1, REF_ADJ_MUSIGN=-1, REF_PERIODIC_X=1, REF_CG_MAX_ITER=21),
+}
+DEFAULT_CG_MAX_ITER = 100000
+
+
+def _sub(pattern: str, repl: str, text: str, count_expected: int, flags=0) -> str:
+    new, n = re.subn(pattern, repl, text, flags=flags)
+    if n != count_expected:
+        raise RuntimeError(f"make_ref: pattern {pattern!r} matched {n} times, expected {count_expected}")
+    return new
+
+
+def _patch_x_boundary(text: str) -> str:
+    """Make the x-boundary branches switchable.  After ``x2 = xup[x]`` the test
+    ``x2 > x`` means "interior" (the periodic case always takes it); after
+    ``x2 = xdn[x]`` it means "wrapped" (the periodic case never takes it)."""
+    out, last, n_up, n_dn = [], None, 0, 0
+    for line in text.split("\n"):
+        if re.search(r"\bx2 = xup\[x\]", line):
+            last = "up"
+        elif re.search(r"\bx2 = xdn\[x\]", line):
+            last = "dn"
+        if re.search(r"\bx2 > x\b", line):
+            if last == "up":
+                line, k = re.subn(r"\bx2 > x\b", "(x2 > x || REF_PERIODIC_X)", line)
+                n_up += k
+            elif last == "dn":
+                line, k = re.subn(r"\bx2 > x\b", "(x2 > x && !REF_PERIODIC_X)", line)
+                n_dn += k
+            else:
+                raise RuntimeError("make_ref: x-boundary test with no preceding x2 assignment")
+        out.append(line)
+    if (n_up, n_dn) != (7, 3):
+        raise RuntimeError(f"make_ref: patched {n_up} forward / {n_dn} backward x-boundary tests, expected 7 / 3")
+    return "\n".join(out)
+
+
+def generate() -> str:
+    """Write oracle/_ref/src/hmc_patched.c (+ RNG files, lapacke stub)."""
+    os.makedirs(SRC, exist_ok=True)
+    with open(os.path.join(REF_ROOT, "hmc.c")) as f:
+        text = f.read()
+    text = _sub(r"^#define NT 32\s*$", "#define NT REF_NT", text, 1, re.M)
+    text = _sub(r"^#define NX 32\s*$", "#define NX REF_NX", text, 1, re.M)
+    text = _sub(r"\bint main\(void\)", "int hmc_reference_main(void)", text, 1)
+    text = _sub(r"^#define CG_MAX_ITER 100000\s*$", "#define CG_MAX_ITER REF_CG_MAX_ITER", text, 1, re.M)
+    # fm_conjugate_mul body: from its signature to the first line that is "}".
+    start = text.index("void fm_conjugate_mul(_Complex double ** v_in")
+    end = text.index("\n}\n", start) + 3
+    body = text[start:end]
+    body = _sub(r"expmu = exp\(mu\);", "expmu = exp(REF_ADJ_MUSIGN*mu);", body, 1)
+    body = _sub(r"expmmu = exp\(-mu\);", "expmmu = exp(-REF_ADJ_MUSIGN*mu);", body, 1)
+    body = _sub(r"v \+= 0\.5 \*", "v += REF_ADJ_SIGN * 0.5 *", body, 4)
+    body = _sub(r"v -= 0\.5 \*", "v -= REF_ADJ_SIGN * 0.5 *", body, 4)
+    text = text[:start] + body + text[end:]
+    text = _patch_x_boundary(text)
+    header = ("/* GENERATED by oracle/make_ref.py from rantahar/Thirring2D hmc.c -- do not edit,\n"
+              " * do not commit.  Test-oracle build only. */\n")
+    with open(os.path.join(SRC, "hmc_patched.c"), "w") as f:
+        f.write(header + text)
+    for name in ("mersenne_inline.c", "mersenne.h"):
+        with open(os.path.join(REF_ROOT, name)) as fi, open(os.path.join(SRC, name), "w") as fo:
+            fo.write(fi.read())
+    # hmc.c includes <lapacke.h> for determinant(), which main never calls.
+    with open(os.path.join(SRC, "lapacke.h"), "w") as f:
+        f.write("/* stub: declares the one LAPACK routine hmc.c names; ref_driver.c defines it to abort() */\n"
+                "void LAPACK_zgetrf(int* m, int* n, _Complex double* a, int* lda, int* ipiv, int* info);\n")
+    return os.path.join(SRC, "hmc_patched.c")
+
+
+def lib_path(nt: int, nx: int, variant: str) -> str:
+    return os.path.join(OUT, f"libhmcref_T{nt}X{nx}_{variant}.so")
+
+
+def build_one(nt: int, nx: int, variant: str) -> str:
+    out = lib_path(nt, nx, variant)
+    driver = os.path.join(HERE, "ref_driver.c")
+    srcs = [driver, os.path.join(SRC, "hmc_patched.c"), os.path.join(SRC, "mersenne_inline.c")]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(s) for s in srcs):
+        return out
+    var = dict(REF_CG_MAX_ITER=DEFAULT_CG_MAX_ITER, **{k: v for k, v in VARIANTS[variant].items()
+                                                      if k != "REF_CG_MAX_ITER"})
+    if "REF_CG_MAX_ITER" in VARIANTS[variant]:
+        var["REF_CG_MAX_ITER"] = VARIANTS[variant]["REF_CG_MAX_ITER"]
+    defs = [f"-DREF_NT={nt}", f"-DREF_NX={nx}"] + [f"-D{k}={v}" for k, v in var.items()]
+    cmd = (["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", "-w", "-Wl,-Bsymbolic", f"-I{SRC}"] + defs
+           + ["-o", out, driver, os.path.join(SRC, "mersenne_inline.c"), "-lm"])
+    subprocess.run(cmd, check=True)
+    return out
+
+
+def available() -> bool:
+    return os.path.exists(os.path.join(SRC, "hmc_patched.c")) or os.path.exists(os.path.join(REF_ROOT, "hmc.c"))
+
+
+def build(sizes=None, variants=None) -> list[str]:
+    """Generate (if the reference tree is present) and compile the oracle/_ref libraries."""
+    if os.path.exists(os.path.join(REF_ROOT, "hmc.c")):
+        generate()
+    elif not os.path.exists(os.path.join(SRC, "hmc_patched.c")):
+        return []
+    sizes = sizes or DEFAULT_SIZES
+    variants = variants or [v for v in VARIANTS if not v.startswith("sample")]
+    jobs = [(nt, nx, v) for (nt, nx) in sizes for v in variants]
+    jobs += [(nt, nx, "sample_px") for (nt, nx) in SAMPLE_SIZES if (nt, nx) in sizes]
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
+        return list(ex.map(lambda j: build_one(*j), jobs))
+
+
+if __name__ == "__main__":
+    sizes = None
+    if len(sys.argv) > 1:
+        sizes = [tuple(int(v) for v in a.lower().split("x")) for a in sys.argv[1:]]
+    for p in build(sizes):
+        print(p)

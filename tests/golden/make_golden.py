@@ -1,0 +1,112 @@
+"""Generate tests/golden/*.npz from the reference hmc.c itself.
+
+Run from the repository root where the reference tree is available:
+
+    python oracle/make_ref.py && python tests/golden/make_golden.py
+
+Each fixture is produced by the adjoint-corrected build of the reference's own
+hmc.c + mersenne_inline.c (oracle/_ref, see oracle/make_ref.py), driven
+in-process through oracle/ref_driver.c.  The reference ships no golden vectors
+or known-answer tests, so these outputs ARE the pins: the CPU oracle is checked
+against them without a GPU, and the CUDA library on the GPU.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import make_ref  # noqa: E402
+from oracle.oracle import RefHMC  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+# name: (nt, nx, m, g, mu, variant, sigma_A, seed, puregauge sweeps, trajectories, nsteps)
+CONFIGS = {
+    # BASELINE C1 shape, reference boundary conditions (x antiperiodic)
+    "c1_16x16_apx": (16, 16, 0.1, 0.5, 0.0, "fixed_apx", 0.1, 12345, 10, 3, 10),
+    # BASELINE C1 boundary conditions (x periodic)
+    "c1_16x16_px": (16, 16, 0.1, 0.5, 0.0, "fixed_px", 0.1, 4242, 10, 3, 10),
+    # C1 shape with a stable step size (40 steps): |dH| < 1, so dH is pinned absolutely
+    "c1s_16x16_px": (16, 16, 0.1, 0.5, 0.0, "fixed_px", 0.1, 2024, 10, 3, 40),
+    # chemical potential on: exercises e^{+-mu} and the stochastic-term force
+    "mu_8x8_px": (8, 8, 0.3, 0.8, 0.3, "fixed_px", 0.3, 777, 5, 3, 10),
+    # odd shape, mu on, reference BCs
+    "odd_6x4_apx": (6, 4, 0.5, 1.0, 0.2, "fixed_apx", 0.5, 99, 5, 3, 8),
+}
+
+MT_SEEDS = [12345, 4354365264, -7]
+
+
+def make_config(name, nt, nx, m, g, mu, variant, sigma, seed, sweeps, ntraj, nsteps):
+    rng = np.random.default_rng(abs(seed) + 1)
+    A = rng.normal(0.0, sigma, (nt, nx, 2))
+    psi = rng.normal(size=(nt, nx)) + 1j * rng.normal(size=(nt, nx))
+    noise = rng.normal(size=(nt, nx)) + 1j * rng.normal(size=(nt, nx))
+    mom0 = rng.normal(size=(nt, nx, 2))
+    ref = RefHMC(nt, nx, m, g, mu, seed=seed, warmup=543210, variant=variant)
+    ref.set_A(A)
+    out = dict(nt=nt, nx=nx, m=m, g=g, mu=mu, bc_x=(1 if variant.endswith("_px") else -1), bc_t=-1,
+               A=A, psi=psi, noise=noise, mom0=mom0)
+    out["M_psi"] = ref.M(psi)
+    out["Mdag_psi"] = ref.Mdag(psi)
+    out["cg_x"] = ref.cg(psi)
+    out["S_gauge"] = ref.gauge_action()
+    out["S_pf"] = ref.pseudofermion_action(psi)
+    out["S_md"] = ref.md_action(noise)
+    out["mom_step"] = ref.momentum_step(mom0, psi, noise, 0.1)
+    # trajectory sequence from the reference's own set-up: seed, 543210
+    # warm-up draws, A = 0, pure-gauge sweeps, then update_gauge's sequence
+    tr = RefHMC(nt, nx, m, g, mu, seed=seed, warmup=543210, variant=variant)
+    tr.puregauge(sweeps)
+    out["traj_seed"] = seed
+    out["traj_sweeps"] = sweeps
+    out["traj_nsteps"] = nsteps
+    out["traj_A_start"] = tr.get_A()
+    stats, As = [], []
+    for _ in range(ntraj):
+        stats.append(tr.trajectory(nsteps, 1.0))
+        As.append(tr.get_A())
+    out["traj_stats"] = np.array(stats)
+    out["traj_A"] = np.array(As)
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+    print(name, "dH", out["traj_stats"][:, 0], "acc", out["traj_stats"][:, 9])
+
+
+def make_mt():
+    out = {}
+    for s in MT_SEEDS:
+        ref = RefHMC(4, 4, 0.1, 0.5, 0.0, seed=s, warmup=543210)
+        out[f"seed_{s}"] = ref.uniforms(3000)
+    ref = RefHMC(4, 4, 0.1, 0.5, 0.0, seed=12345, warmup=0)
+    out["seed_12345_nowarmup"] = ref.uniforms(1300)
+    np.savez_compressed(os.path.join(OUT, "mt_stream.npz"), **out)
+
+
+def make_dense():
+    out = {}
+    for name, (nt, nx, m, mu, variant) in {"det_4x4_apx": (4, 4, 0.2, 0.1, "fixed_apx"),
+                                           "det_4x4_px": (4, 4, 0.05, 0.0, "fixed_px"),
+                                           "det_6x4_apx": (6, 4, 0.3, 0.25, "fixed_apx")}.items():
+        rng = np.random.default_rng(nt * 100 + nx)
+        A = rng.normal(0, 0.4, (nt, nx, 2))
+        ref = RefHMC(nt, nx, m, 0.5, mu, variant=variant, warmup=0)
+        ref.set_A(A)
+        Md = ref.dense_M()
+        sign, logdet = np.linalg.slogdet(Md)
+        out[name] = dict(nt=nt, nx=nx, m=m, mu=mu, bc_x=(1 if variant.endswith("_px") else -1), A=A, M=Md,
+                         logabsdet=logdet, phase=sign)
+    for name, d in out.items():
+        np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **d)
+
+
+if __name__ == "__main__":
+    make_ref.build([(c[0], c[1]) for c in CONFIGS.values()] + [(4, 4), (6, 4)])
+    make_mt()
+    make_dense()
+    for name, cfg in CONFIGS.items():
+        make_config(name, *cfg)

@@ -1,0 +1,47 @@
+"""The C-ABI libraries build, load without a GPU and export every entry point
+their headers declare.  No compute calls (this suite runs without a GPU)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(header: str) -> list[str]:
+    with open(os.path.join(ROOT, "include", header)) as f:
+        text = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", text, flags=re.M)
+    return sorted(set(n for n in names if n not in ("if", "while", "for", "return", "sizeof")))
+
+
+def exported(lib: str) -> set[str]:
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], check=True, stdout=subprocess.PIPE, text=True).stdout
+    return {line.split()[-1] for line in out.splitlines() if line.split()}
+
+
+@pytest.fixture(scope="module")
+def built():
+    from thirring2d_gb300 import build
+    return build.build()
+
+
+def test_gpu_library_exports(built):
+    names = declared("thirring_gpu.h")
+    assert len(names) >= 25
+    missing = [n for n in names if n not in exported(built["libthirring_gpu"])]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(built):
+    from thirring2d_gb300 import native
+    assert set(declared("thirring_gpu.h")) == set(native.SIGNATURES)
+
+
+def test_library_loads_without_gpu(built):
+    lib = ctypes.CDLL(built["libthirring_gpu"])
+    lib.tg_version.restype = ctypes.c_char_p
+    assert b"sm_103a" in lib.tg_version()
+

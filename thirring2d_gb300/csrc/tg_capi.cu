@@ -1,0 +1,876 @@
+// tg_capi.cu -- host side of the Thirring2D GB300 library: lattice context,
+// reference RNG stream, CG and trajectory scheduling (CUDA graphs with
+// conditional WHILE/IF nodes, or eager launches with host polling), and the
+// C ABI declared in include/thirring_gpu.h.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "tg_launch.h"
+
+using namespace tg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define TG_CK(call)                                                                                    \
+  do {                                                                                                 \
+    cudaError_t e_ = (call);                                                                           \
+    if (e_ != cudaSuccess)                                                                             \
+      return fail(TG_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + " (" __FILE__ ":" + \
+                                 std::to_string(__LINE__) + ")");                                      \
+  } while (0)
+
+#define TG_TRY(expr)          \
+  do {                        \
+    int rc_ = (expr);         \
+    if (rc_ != TG_OK) return rc_; \
+  } while (0)
+
+constexpr int kMaxPf = 8;
+constexpr int kMaxLog = 4096;
+
+// ---------------------------------------------------------------------------
+// The reference's random stream: MT19937 (Matsumoto & Nishimura 1998) seeded
+// by the Knuth 69069 recurrence from an odd seed, each block of 624 tempered
+// words handed out last-first as y * 2^-32 (mersenne_inline.c:73-128,
+// mersenne.h:11).  Box-Muller pairs as hmc.c:423-426.
+// ---------------------------------------------------------------------------
+struct RefStream {
+  uint32_t w[624];
+  double out[624];
+  int avail = 0;
+
+  void seed(long s) {
+    if (s % 2 == 0) s++;
+    w[0] = (uint32_t)(s & 0xffffffffL);
+    for (int i = 1; i < 624; i++) w[i] = 69069u * w[i - 1];
+    avail = 0;
+  }
+  void twist() {
+    for (int i = 0; i < 624; i++) {
+      uint32_t y = (w[i] & 0x80000000u) | (w[i + 1 < 624 ? i + 1 : 0] & 0x7fffffffu);
+      uint32_t n = w[i + 397 < 624 ? i + 397 : i + 397 - 624] ^ (y >> 1);
+      w[i] = (y & 1u) ? n ^ 0x9908b0dfu : n;
+    }
+    for (int i = 0; i < 624; i++) {
+      uint32_t y = w[i];
+      y ^= y >> 11;
+      y ^= (y << 7) & 0x9d2c5680u;
+      y ^= (y << 15) & 0xefc60000u;
+      y ^= y >> 18;
+      out[i] = (double)y * (1.0 / 4294967296.0);
+    }
+    avail = 624;
+  }
+  double next() {
+    if (avail == 0) twist();
+    return out[--avail];
+  }
+  void gauss_pairs(long n, double* dst) {  // dst[2n]
+    for (long k = 0; k < n; k++) {
+      double u1 = next(), u2 = next();
+      double r = sqrt(-2 * log(u1));
+      dst[2 * k] = r * cos(2 * M_PI * u2);
+      dst[2 * k + 1] = r * sin(2 * M_PI * u2);
+    }
+  }
+};
+
+struct GraphEntry {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+}  // namespace
+
+struct tg_lattice {
+  tg_lattice_params P{};
+  Geo g{};
+  int V = 0;
+  int version = 0;  // bumped when couplings change (invalidates graphs)
+  cudaStream_t stream = nullptr, cap2 = nullptr, cap3 = nullptr;
+
+  double2 *A = nullptr, *Anew = nullptr, *Wt = nullptr, *Wx = nullptr;
+  float2 *Wt32 = nullptr, *Wx32 = nullptr;
+  double2 *mom = nullptr, *noise = nullptr, *chi = nullptr, *Mchi = nullptr, *vin = nullptr, *vout = nullptr;
+  double2 *eta = nullptr, *phi = nullptr;  // [npf_alloc][V]
+  int npf_alloc = 0;
+  CgBufs64 w64{};
+  CgBufsMixed wmx{};
+  CgState* st = nullptr;
+  CgLog* log = nullptr;
+  TrajStats* ts = nullptr;
+  Red red{};
+
+  double* h_stage = nullptr;  // pinned, 2*V*kMaxPf doubles... sized at create
+  size_t h_stage_len = 0;
+  CgState* h_st = nullptr;
+  TrajStats* h_ts = nullptr;
+  CgLog* h_log = nullptr;
+
+  RefStream mt;
+  bool mt_seeded = false;
+  std::map<std::string, GraphEntry> graphs;
+  std::vector<cudaEvent_t> ev;
+};
+
+namespace {
+
+OpK<double> op_k(const tg_lattice* L, int dagger) {
+  double ep = exp(L->P.mu), em = exp(-L->P.mu);
+  OpK<double> k;
+  k.m = L->P.m;
+  if (!dagger) { k.cf = ep; k.cb = -em; k.cx = 1.0; }
+  else { k.cf = -em; k.cb = ep; k.cx = -1.0; }
+  return k;
+}
+OpK<float> op_k32(const tg_lattice* L, int dagger) {
+  OpK<double> k = op_k(L, dagger);
+  OpK<float> f;
+  f.m = (float)k.m; f.cf = (float)k.cf; f.cb = (float)k.cb; f.cx = (float)k.cx;
+  return f;
+}
+Links links(const tg_lattice* L) { return Links{L->Wt, L->Wx, L->Wt32, L->Wx32}; }
+
+bool env_graph_enabled() {
+  const char* e = getenv("TG_GRAPH");
+  return !(e && e[0] == '0');
+}
+
+template <typename T> int dmalloc(T** p, size_t n) {
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) return fail(TG_E_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return TG_OK;
+}
+
+int ensure_pf(tg_lattice* L, int npf) {
+  if (npf <= L->npf_alloc) return TG_OK;
+  if (npf > kMaxPf) return fail(TG_E_ARG, "npf > 8");
+  TG_CK(cudaStreamSynchronize(L->stream));
+  if (L->eta) cudaFree(L->eta);
+  if (L->phi) cudaFree(L->phi);
+  L->eta = L->phi = nullptr;
+  TG_TRY(dmalloc(&L->eta, (size_t)npf * L->V));
+  TG_TRY(dmalloc(&L->phi, (size_t)npf * L->V));
+  L->npf_alloc = npf;
+  for (auto& kv : L->graphs) {  // graphs hold the old pointers
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  L->graphs.clear();
+  return TG_OK;
+}
+
+int ensure_events(tg_lattice* L, size_t n) {
+  while (L->ev.size() < n) {
+    cudaEvent_t e;
+    TG_CK(cudaEventCreate(&e));
+    L->ev.push_back(e);
+  }
+  return TG_OK;
+}
+
+int check_cg_params(const tg_cg_params* cp) {
+  if (!cp) return fail(TG_E_ARG, "null CG parameters");
+  if (cp->maxiter <= 0) return fail(TG_E_ARG, "maxiter must be positive");
+  if (cp->precision != TG_PREC_FP64 && cp->precision != TG_PREC_MIXED) return fail(TG_E_ARG, "bad precision");
+  if (cp->precision == TG_PREC_MIXED && cp->ru_interval <= 0) return fail(TG_E_ARG, "ru_interval must be positive");
+  if (!(cp->rel_tol >= 0) || !(cp->abs_tol2 >= 0)) return fail(TG_E_ARG, "tolerances must be >= 0");
+  return TG_OK;
+}
+
+// Add a conditional node after the current capture dependencies of `s` and
+// return its body graph; the capture continues after the node.
+int add_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                    cudaGraph_t* body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t gr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  TG_CK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &gr, &deps, nullptr, &nd));
+  if (cs != cudaStreamCaptureStatusActive) return fail(TG_E_CUDA, "stream is not capturing");
+  // cudaGraphNodeParams has no usable default constructor in C++; zero it as bytes
+  alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)] = {};
+  cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(raw);
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = type;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  TG_CK(cudaGraphAddNode(&node, gr, deps, nullptr, nd, &np));
+  TG_CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  *body = np.conditional.phGraph_out[0];
+  return TG_OK;
+}
+
+int capture_graph_of(cudaStream_t s, cudaGraph_t* gr) {
+  cudaStreamCaptureStatus cs;
+  TG_CK(cudaStreamGetCaptureInfo(s, &cs, nullptr, gr, nullptr, nullptr, nullptr));
+  return TG_OK;
+}
+
+// Enqueue one CG solve of M^dag M x = b on stream s.  graph = true: s is
+// capturing and the iteration loop becomes a conditional WHILE node (no host
+// involvement at run time).  graph = false: iterations are launched in
+// chunks and the host polls the device `done` flag between chunks.
+int enqueue_cg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const double2* b, double2* x, int log_index,
+               bool graph) {
+  const Geo& g = L->g;
+  const bool mixed = cp.precision == TG_PREC_MIXED;
+  OpK<double> km = op_k(L, 0), kd = op_k(L, 1);
+  OpK<float> km32 = op_k32(L, 0), kd32 = op_k32(L, 1);
+  Links lk = links(L);
+  if (graph) {
+    cudaGraph_t top;
+    TG_TRY(capture_graph_of(s, &top));
+    cudaGraphConditionalHandle hloop;
+    TG_CK(cudaGraphConditionalHandleCreate(&hloop, top, 0, 0));
+    Cond c0{hloop, 0, 1};
+    if (mixed)
+      cgmx_init(s, g, b, x, L->wmx, L->st, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, cp.ru_interval, log_index,
+                c0);
+    else
+      cg64_init(s, g, b, x, L->w64, L->st, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, log_index, c0);
+    TG_CK(cudaGetLastError());
+    cudaGraph_t body;
+    TG_TRY(add_conditional(s, hloop, cudaGraphCondTypeWhile, &body));
+    TG_CK(cudaStreamBeginCaptureToGraph(L->cap2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    if (!mixed) {
+      cg64_iter(L->cap2, g, km, kd, lk, x, L->w64, L->st, L->log, L->red, c0);
+    } else {
+      cudaGraphConditionalHandle hru;
+      TG_CK(cudaGraphConditionalHandleCreate(&hru, body, 0, 0));
+      Cond c1{hloop, hru, 1};
+      cgmx_iter(L->cap2, g, km32, kd32, lk, L->wmx, L->st, L->red, c1);
+      cudaGraph_t ifbody;
+      TG_TRY(add_conditional(L->cap2, hru, cudaGraphCondTypeIf, &ifbody));
+      TG_CK(cudaStreamBeginCaptureToGraph(L->cap3, ifbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+      cgmx_reliable(L->cap3, g, km, kd, lk, b, x, L->wmx, L->st, L->log, L->red, c1);
+      TG_CK(cudaGetLastError());
+      cudaGraph_t tmp;
+      TG_CK(cudaStreamEndCapture(L->cap3, &tmp));
+    }
+    TG_CK(cudaGetLastError());
+    cudaGraph_t tmp;
+    TG_CK(cudaStreamEndCapture(L->cap2, &tmp));
+    return TG_OK;
+  }
+  Cond none{0, 0, 0};
+  if (mixed)
+    cgmx_init(s, g, b, x, L->wmx, L->st, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, cp.ru_interval, log_index,
+              none);
+  else
+    cg64_init(s, g, b, x, L->w64, L->st, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, log_index, none);
+  TG_CK(cudaGetLastError());
+  const int chunk = 16;
+  long max_chunks = (long)cp.maxiter / chunk + 2;
+  for (long c = 0; c < max_chunks; c++) {
+    TG_CK(cudaMemcpyAsync(L->h_st, L->st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+    TG_CK(cudaStreamSynchronize(s));
+    if (L->h_st->done) return TG_OK;
+    for (int j = 0; j < chunk; j++) {
+      if (!mixed) {
+        cg64_iter(s, g, km, kd, lk, x, L->w64, L->st, L->log, L->red, none);
+      } else {
+        cgmx_iter(s, g, km32, kd32, lk, L->wmx, L->st, L->red, none);
+        cgmx_reliable(s, g, km, kd, lk, b, x, L->wmx, L->st, L->log, L->red, none);
+      }
+    }
+    TG_CK(cudaGetLastError());
+  }
+  TG_CK(cudaMemcpyAsync(L->h_st, L->st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+  TG_CK(cudaStreamSynchronize(s));
+  if (!L->h_st->done) return fail(TG_E_NOCONV, "CG loop did not terminate");
+  return TG_OK;
+}
+
+// Run `fn(stream, graph)` either as a cached CUDA graph (key) or eagerly.
+template <typename F> int run_maybe_graph(tg_lattice* L, const std::string& key, bool use_graph, F fn) {
+  if (!use_graph) return fn(L->stream, false);
+  auto it = L->graphs.find(key);
+  if (it == L->graphs.end()) {
+    GraphEntry ge;
+    TG_CK(cudaStreamBeginCapture(L->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = fn(L->stream, true);
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamEndCapture(L->stream, &gr);
+    if (rc != TG_OK) {
+      if (gr) cudaGraphDestroy(gr);
+      return rc;
+    }
+    if (e != cudaSuccess) return fail(TG_E_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    ge.graph = gr;
+    TG_CK(cudaGraphInstantiate(&ge.exec, gr, 0));
+    it = L->graphs.emplace(key, ge).first;
+  }
+  TG_CK(cudaGraphLaunch(it->second.exec, L->stream));
+  return TG_OK;
+}
+
+std::string cg_key(const tg_cg_params& cp) {
+  char buf[160];
+  snprintf(buf, sizeof buf, "%.17g/%.17g/%d/%d/%d", cp.rel_tol, cp.abs_tol2, cp.maxiter, cp.precision,
+           cp.ru_interval);
+  return buf;
+}
+
+int read_cg_result(tg_lattice* L, tg_cg_result* res) {
+  TG_CK(cudaMemcpyAsync(L->h_st, L->st, sizeof(CgState), cudaMemcpyDeviceToHost, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  if (res) {
+    res->iterations = L->h_st->iter;
+    res->status = L->h_st->status;
+    res->reliable_updates = L->h_st->n_ru;
+    res->rr = L->h_st->rr;
+    res->rr0 = L->h_st->rr0;
+  }
+  return TG_OK;
+}
+
+// Solve on device vectors b -> x (both double2[V]) with the lattice's links.
+int solve_dev(tg_lattice* L, const tg_cg_params& cp, const double2* b, double2* x, tg_cg_result* res) {
+  std::string key = "cg:" + cg_key(cp) + ":" + std::to_string((uintptr_t)b) + ":" + std::to_string((uintptr_t)x) +
+                    ":" + std::to_string(L->version);
+  TG_TRY(run_maybe_graph(L, key, env_graph_enabled(),
+                         [&](cudaStream_t s, bool graph) { return enqueue_cg(L, s, cp, b, x, -1, graph); }));
+  TG_TRY(read_cg_result(L, res));
+  return TG_OK;
+}
+
+// A finished solve that did not converge is reported as the call's status
+// (the outputs are still written), with a message for tg_last_error().
+int solver_status(int status) {
+  switch (status) {
+    case TG_OK: return TG_OK;
+    case TG_E_NOCONV: return fail(TG_E_NOCONV, "CG reached its iteration cap");
+    case TG_E_DIVERGED: return fail(TG_E_DIVERGED, "Cannot invert fermion matrix (|r|^2/|r0|^2 > 1e10)");
+    case TG_E_NAN: return fail(TG_E_NAN, "NaN in the CG recurrence");
+    default: return fail(status, "solver error");
+  }
+}
+
+int upload(tg_lattice* L, void* dst, const double* src, size_t ndouble) {
+  if (ndouble > L->h_stage_len) return fail(TG_E_ARG, "field larger than staging buffer");
+  memcpy(L->h_stage, src, ndouble * sizeof(double));
+  TG_CK(cudaMemcpyAsync(dst, L->h_stage, ndouble * sizeof(double), cudaMemcpyHostToDevice, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));  // staging buffer is reused
+  return TG_OK;
+}
+int download(tg_lattice* L, double* dst, const void* src, size_t ndouble) {
+  if (ndouble > L->h_stage_len) return fail(TG_E_ARG, "field larger than staging buffer");
+  TG_CK(cudaMemcpyAsync(L->h_stage, src, ndouble * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  memcpy(dst, L->h_stage, ndouble * sizeof(double));
+  return TG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// One trajectory (hmc.c:671-746) on the device.  The random fields are in
+// L->eta[0..npf), L->mom, L->noise and L->ts->u already, or are drawn here
+// from Philox (rng == TG_RNG_PHILOX).
+// ---------------------------------------------------------------------------
+int enqueue_trajectory(tg_lattice* L, cudaStream_t s, const tg_hmc_params& p, bool graph) {
+  const Geo& g = L->g;
+  const int V = L->V;
+  const bool use_noise = p.stochastic_term != 0;
+  OpK<double> km = op_k(L, 0), kd = op_k(L, 1);
+  const double ep = exp(L->P.mu), em = exp(-L->P.mu);
+  TrajStats* ts = L->ts;
+  int solve = 0;
+  auto rec = [&](int i) -> int {
+    TG_CK(cudaEventRecordWithFlags(L->ev[i], s, graph ? cudaEventRecordExternal : cudaEventRecordDefault));
+    return TG_OK;
+  };
+  auto cg = [&](const double2* b, double2* x) -> int {
+    TG_TRY(rec(2 * solve));
+    TG_TRY(enqueue_cg(L, s, p.cg, b, x, solve, graph));
+    TG_TRY(rec(2 * solve + 1));
+    solve++;
+    return TG_OK;
+  };
+  if (p.rng == TG_RNG_PHILOX) {
+    for (int k = 0; k < p.npf; k++) philox_gauss(s, V, p.seed, ts, (unsigned)k, L->eta + (size_t)k * V);
+    philox_gauss(s, V, p.seed, ts, 16u, L->mom);
+    if (use_noise) philox_gauss(s, V, p.seed, ts, 17u, L->noise);
+    philox_uniform(s, p.seed, ts, 18u);
+  }
+  link_phase(s, g, L->P.bc_t, L->P.bc_x, L->A, L->Wt, L->Wx, L->Wt32, L->Wx32);
+  // start: S_pf = |eta|^2 exactly (phi = M^dag eta), hmc.c:418-436
+  TG_CK(cudaMemsetAsync(&ts->Spf0, 0, sizeof(double), s));
+  for (int k = 0; k < p.npf; k++) {
+    norm2(s, V, L->eta + (size_t)k * V, &ts->Spf0, 1, L->red);
+    dslash64(s, g, kd, L->eta + (size_t)k * V, L->phi + (size_t)k * V, L->Wt, L->Wx);
+  }
+  norm2(s, V, L->mom, &ts->Smom0, 0, L->red);
+  gauge_action(s, V, L->A, kNf / L->P.g, &ts->Sg0, L->red);
+  if (use_noise) md_action(s, g, kd, L->noise, L->Wt, L->Wx, &ts->Smd0, L->red);
+  else TG_CK(cudaMemsetAsync(&ts->Smd0, 0, sizeof(double), s));
+  TG_CK(cudaMemcpyAsync(L->Anew, L->A, (size_t)V * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  // leapfrog, hmc.c:708-716; the two half steps between MD steps share a launch
+  const double eps = p.tau / p.nsteps;
+  const double c = 2.0 * (p.tau * 0.5 / p.nsteps);
+  const double gfac = eps * kNf / L->P.g;
+  for (int i = 0; i < p.nsteps; i++) {
+    gauge_step(s, g, L->P.bc_t, L->P.bc_x, L->Anew, L->mom, c, i == 0 ? 1 : 2, L->Wt, L->Wx, L->Wt32, L->Wx32);
+    if (p.npf == 0)
+      momentum_update(s, g, ep, em, L->Anew, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->mom, eps, gfac,
+                      1 | (use_noise ? 2 : 0));
+    for (int k = 0; k < p.npf; k++) {
+      TG_TRY(cg(L->phi + (size_t)k * V, L->chi));
+      dslash64(s, g, km, L->chi, L->Mchi, L->Wt, L->Wx);
+      int flags = (k == 0 ? 1 : 0) | ((k == p.npf - 1 && use_noise) ? 2 : 0);
+      momentum_update(s, g, ep, em, L->Anew, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->mom, eps, gfac, flags);
+    }
+  }
+  gauge_step(s, g, L->P.bc_t, L->P.bc_x, L->Anew, L->mom, c, 1, L->Wt, L->Wx, L->Wt32, L->Wx32);
+  // end actions, hmc.c:719-726
+  TG_CK(cudaMemsetAsync(&ts->Spf1, 0, sizeof(double), s));
+  for (int k = 0; k < p.npf; k++) {
+    TG_TRY(cg(L->phi + (size_t)k * V, L->chi));
+    redot(s, V, L->phi + (size_t)k * V, L->chi, &ts->Spf1, 1, L->red);
+  }
+  norm2(s, V, L->mom, &ts->Smom1, 0, L->red);
+  gauge_action(s, V, L->Anew, kNf / L->P.g, &ts->Sg1, L->red);
+  if (use_noise) md_action(s, g, kd, L->noise, L->Wt, L->Wx, &ts->Smd1, L->red);
+  else TG_CK(cudaMemsetAsync(&ts->Smd1, 0, sizeof(double), s));
+  finish_trajectory(s, ts);
+  accept_copy(s, V, ts, L->A, L->Anew);
+  link_phase(s, g, L->P.bc_t, L->P.bc_x, L->A, L->Wt, L->Wx, L->Wt32, L->Wx32);
+  TG_CK(cudaGetLastError());
+  return TG_OK;
+}
+
+int check_hmc_params(const tg_hmc_params* p) {
+  if (!p) return fail(TG_E_ARG, "null HMC parameters");
+  if (p->nsteps <= 0 || !(p->tau > 0)) return fail(TG_E_ARG, "nsteps and tau must be positive");
+  if (p->npf < 0 || p->npf > kMaxPf) return fail(TG_E_ARG, "npf must be in [0, 8]");
+  if ((p->nsteps + 1) * (p->npf > 0 ? p->npf : 1) > kMaxLog) return fail(TG_E_ARG, "too many CG solves");
+  return check_cg_params(&p->cg);
+}
+
+int run_trajectory(tg_lattice* L, const tg_hmc_params& p, tg_traj_result* r) {
+  TG_TRY(ensure_pf(L, p.npf > 0 ? p.npf : 1));
+  const int nsolves = (p.nsteps + 1) * p.npf;
+  TG_TRY(ensure_events(L, 2 * (size_t)nsolves + 2));
+  char buf[256];
+  snprintf(buf, sizeof buf, "traj:%d/%.17g/%d/%d/%d/%llu/%d:", p.nsteps, p.tau, p.npf, p.stochastic_term, p.rng,
+           (unsigned long long)p.seed, L->version);
+  std::string key = buf + cg_key(p.cg);
+  bool use_graph = p.use_graph && env_graph_enabled();
+  TG_TRY(run_maybe_graph(L, key, use_graph, [&](cudaStream_t s, bool graph) {
+    return enqueue_trajectory(L, s, p, graph);
+  }));
+  TG_CK(cudaMemcpyAsync(L->h_ts, L->ts, sizeof(TrajStats), cudaMemcpyDeviceToHost, L->stream));
+  if (nsolves > 0)
+    TG_CK(cudaMemcpyAsync(L->h_log, L->log, sizeof(CgLog) * nsolves, cudaMemcpyDeviceToHost, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  if (r) {
+    const TrajStats& t = *L->h_ts;
+    memset(r, 0, sizeof(*r));
+    r->dH = t.dH;
+    r->Sg0 = t.Sg0; r->Spf0 = t.Spf0; r->Smd0 = t.Smd0; r->Smom0 = t.Smom0;
+    r->Sg1 = t.Sg1; r->Spf1 = t.Spf1; r->Smd1 = t.Smd1; r->Smom1 = t.Smom1;
+    r->u_accept = t.u;
+    r->accepted = t.accepted;
+    r->cg_solves = nsolves;
+    double ms = 0;
+    for (int i = 0; i < nsolves; i++) {
+      const CgLog& l = L->h_log[i];
+      r->cg_iterations += l.iter;
+      if (l.iter > r->cg_max_iterations) r->cg_max_iterations = l.iter;
+      r->reliable_updates += l.n_ru;
+      if (l.status > r->status) r->status = l.status;
+      float e = 0;
+      if (cudaEventElapsedTime(&e, L->ev[2 * i], L->ev[2 * i + 1]) == cudaSuccess) ms += e;
+    }
+    r->cg_ms = ms;
+    return solver_status(r->status);
+  }
+  return TG_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* tg_last_error(void) { return g_err.c_str(); }
+const char* tg_version(void) { return "thirring2d_gb300 0.1 (sm_103a)"; }
+
+int tg_create(const tg_lattice_params* p, tg_lattice** out) {
+  if (!p || !out) return fail(TG_E_ARG, "null argument");
+  *out = nullptr;
+  if (p->nt < 2 || p->nx < 2) return fail(TG_E_ARG, "lattice sides must be >= 2");
+  long long V = (long long)p->nt * p->nx;
+  if (V >= (1LL << 24)) return fail(TG_E_ARG, "volume must be below 2^24 sites");
+  auto bc_ok = [](int b) { return b == 1 || b == -1 || b == 0; };
+  if (!bc_ok(p->bc_t) || !bc_ok(p->bc_x)) return fail(TG_E_ARG, "boundary conditions must be -1, 0 or 1");
+  if (!(p->g > 0)) return fail(TG_E_ARG, "g must be positive");
+  TG_CK(cudaSetDevice(p->device));
+  tg_lattice* L = new tg_lattice();
+  L->P = *p;
+  L->V = (int)V;
+  L->g.nt = p->nt;
+  L->g.nx = p->nx;
+  L->g.V = (int)V;
+  L->g.inv_nx = 1.0f / (float)p->nx;
+  auto bail = [&](int rc) { tg_destroy(L); return rc; };
+  if (cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&L->cap2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&L->cap3, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(TG_E_CUDA, "stream creation failed"));
+  size_t n = (size_t)V;
+  int rc = TG_OK;
+  double2** d2[] = {&L->A, &L->Anew, &L->Wt, &L->Wx, &L->mom, &L->noise, &L->chi, &L->Mchi, &L->vin, &L->vout,
+                    &L->w64.r, &L->w64.p, &L->w64.Mp, &L->wmx.tmp64};
+  for (auto pp : d2)
+    if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
+  float2** f2[] = {&L->Wt32, &L->Wx32, &L->wmx.xs, &L->wmx.rs, &L->wmx.ps, &L->wmx.Mps};
+  for (auto pp : f2)
+    if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
+  if ((rc = dmalloc(&L->st, 1)) != TG_OK || (rc = dmalloc(&L->log, kMaxLog)) != TG_OK ||
+      (rc = dmalloc(&L->ts, 1)) != TG_OK || (rc = dmalloc(&L->red.partials, (size_t)nblocks((int)V) + 32)) != TG_OK ||
+      (rc = dmalloc(&L->red.counter, 1)) != TG_OK)
+    return bail(rc);
+  if ((rc = ensure_pf(L, 1)) != TG_OK) return bail(rc);
+  L->h_stage_len = (size_t)(kMaxPf + 2) * 2 * n;  // npf eta fields + momenta + noise
+  if (cudaMallocHost((void**)&L->h_stage, L->h_stage_len * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost((void**)&L->h_st, sizeof(CgState)) != cudaSuccess ||
+      cudaMallocHost((void**)&L->h_ts, sizeof(TrajStats)) != cudaSuccess ||
+      cudaMallocHost((void**)&L->h_log, sizeof(CgLog) * kMaxLog) != cudaSuccess)
+    return bail(fail(TG_E_ALLOC, "pinned host allocation failed"));
+  if (cudaMemsetAsync(L->A, 0, n * sizeof(double2), L->stream) != cudaSuccess ||
+      cudaMemsetAsync(L->noise, 0, n * sizeof(double2), L->stream) != cudaSuccess ||
+      cudaMemsetAsync(L->red.counter, 0, sizeof(unsigned), L->stream) != cudaSuccess ||
+      cudaMemsetAsync(L->ts, 0, sizeof(TrajStats), L->stream) != cudaSuccess ||
+      cudaMemsetAsync(L->st, 0, sizeof(CgState), L->stream) != cudaSuccess)
+    return bail(fail(TG_E_CUDA, "initial memset failed"));
+  link_phase(L->stream, L->g, p->bc_t, p->bc_x, L->A, L->Wt, L->Wx, L->Wt32, L->Wx32);
+  if (cudaStreamSynchronize(L->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return bail(fail(TG_E_CUDA, "initialisation kernels failed"));
+  L->mt.seed(0);
+  *out = L;
+  return TG_OK;
+}
+
+int tg_destroy(tg_lattice* L) {
+  if (!L) return TG_OK;
+  cudaSetDevice(L->P.device);
+  if (L->stream) cudaStreamSynchronize(L->stream);
+  for (auto& kv : L->graphs) {
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  for (auto e : L->ev) cudaEventDestroy(e);
+  void* dev[] = {L->A, L->Anew, L->Wt, L->Wx, L->mom, L->noise, L->chi, L->Mchi, L->vin, L->vout, L->w64.r,
+                 L->w64.p, L->w64.Mp, L->wmx.tmp64, L->Wt32, L->Wx32, L->wmx.xs, L->wmx.rs, L->wmx.ps, L->wmx.Mps,
+                 L->st, L->log, L->ts, L->red.partials, L->red.counter, L->eta, L->phi};
+  for (void* d : dev)
+    if (d) cudaFree(d);
+  void* hst[] = {L->h_stage, L->h_st, L->h_ts, L->h_log};
+  for (void* h : hst)
+    if (h) cudaFreeHost(h);
+  if (L->stream) cudaStreamDestroy(L->stream);
+  if (L->cap2) cudaStreamDestroy(L->cap2);
+  if (L->cap3) cudaStreamDestroy(L->cap3);
+  delete L;
+  return TG_OK;
+}
+
+int tg_set_couplings(tg_lattice* L, double m, double g, double mu) {
+  if (!L) return fail(TG_E_ARG, "null lattice");
+  if (!(g > 0)) return fail(TG_E_ARG, "g must be positive");
+  L->P.m = m;
+  L->P.g = g;
+  L->P.mu = mu;
+  L->version++;
+  return TG_OK;
+}
+
+int tg_get_params(const tg_lattice* L, tg_lattice_params* p) {
+  if (!L || !p) return fail(TG_E_ARG, "null argument");
+  *p = L->P;
+  return TG_OK;
+}
+
+int tg_synchronize(tg_lattice* L) {
+  if (!L) return fail(TG_E_ARG, "null lattice");
+  TG_CK(cudaStreamSynchronize(L->stream));
+  return TG_OK;
+}
+
+void* tg_stream(tg_lattice* L) { return L ? (void*)L->stream : nullptr; }
+
+int tg_set_gauge(tg_lattice* L, const double* A) {
+  if (!L || !A) return fail(TG_E_ARG, "null argument");
+  TG_TRY(upload(L, L->A, A, 2 * (size_t)L->V));
+  link_phase(L->stream, L->g, L->P.bc_t, L->P.bc_x, L->A, L->Wt, L->Wx, L->Wt32, L->Wx32);
+  TG_CK(cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_set_gauge_dev(tg_lattice* L, const void* A_dev) {
+  if (!L || !A_dev) return fail(TG_E_ARG, "null argument");
+  TG_CK(cudaMemcpyAsync(L->A, A_dev, (size_t)L->V * sizeof(double2), cudaMemcpyDeviceToDevice, L->stream));
+  link_phase(L->stream, L->g, L->P.bc_t, L->P.bc_x, L->A, L->Wt, L->Wx, L->Wt32, L->Wx32);
+  TG_CK(cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_get_gauge(tg_lattice* L, double* A) {
+  if (!L || !A) return fail(TG_E_ARG, "null argument");
+  return download(L, A, L->A, 2 * (size_t)L->V);
+}
+
+int tg_apply(tg_lattice* L, const double* in, double* out, int dagger) {
+  if (!L || !in || !out) return fail(TG_E_ARG, "null argument");
+  TG_TRY(upload(L, L->vin, in, 2 * (size_t)L->V));
+  dslash64(L->stream, L->g, op_k(L, dagger), L->vin, L->vout, L->Wt, L->Wx);
+  TG_CK(cudaGetLastError());
+  return download(L, out, L->vout, 2 * (size_t)L->V);
+}
+
+int tg_apply_dev(tg_lattice* L, const void* in, void* out, int dagger, int precision) {
+  if (!L || !in || !out) return fail(TG_E_ARG, "null argument");
+  if (precision == TG_PREC_FP64)
+    dslash64(L->stream, L->g, op_k(L, dagger), (const double2*)in, (double2*)out, L->Wt, L->Wx);
+  else if (precision == TG_PREC_MIXED)
+    dslash32(L->stream, L->g, op_k32(L, dagger), (const float2*)in, (float2*)out, L->Wt32, L->Wx32);
+  else
+    return fail(TG_E_ARG, "bad precision");
+  TG_CK(cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_time_apply(tg_lattice* L, int n, int dagger, int precision, double* ms_per_apply) {
+  if (!L || n <= 0 || !ms_per_apply) return fail(TG_E_ARG, "bad argument");
+  TG_TRY(ensure_events(L, 2));
+  cudaEvent_t e0 = L->ev[0], e1 = L->ev[1];
+  TG_CK(cudaEventRecord(e0, L->stream));
+  for (int i = 0; i < n; i++) {
+    // ping-pong between two buffers so every apply reads the previous output
+    if (precision == TG_PREC_FP64) {
+      const double2* in = (i & 1) ? L->vout : L->vin;
+      double2* out = (i & 1) ? L->vin : L->vout;
+      dslash64(L->stream, L->g, op_k(L, dagger), in, out, L->Wt, L->Wx);
+    } else {
+      const float2* in = (i & 1) ? L->wmx.Mps : L->wmx.ps;
+      float2* out = (i & 1) ? L->wmx.ps : L->wmx.Mps;
+      dslash32(L->stream, L->g, op_k32(L, dagger), in, out, L->Wt32, L->Wx32);
+    }
+  }
+  TG_CK(cudaEventRecord(e1, L->stream));
+  TG_CK(cudaEventSynchronize(e1));
+  TG_CK(cudaGetLastError());
+  float ms = 0;
+  TG_CK(cudaEventElapsedTime(&ms, e0, e1));
+  *ms_per_apply = ms / n;
+  return TG_OK;
+}
+
+int tg_cg(tg_lattice* L, const tg_cg_params* cp, const double* b, double* x, tg_cg_result* res) {
+  if (!L || !b || !x) return fail(TG_E_ARG, "null argument");
+  TG_TRY(check_cg_params(cp));
+  TG_TRY(upload(L, L->vin, b, 2 * (size_t)L->V));
+  tg_cg_result r{};
+  TG_TRY(solve_dev(L, *cp, L->vin, L->vout, &r));
+  if (res) *res = r;
+  TG_TRY(download(L, x, L->vout, 2 * (size_t)L->V));
+  return solver_status(r.status);
+}
+
+int tg_cg_dev(tg_lattice* L, const tg_cg_params* cp, const void* b_dev, void* x_dev, tg_cg_result* res) {
+  if (!L || !b_dev || !x_dev) return fail(TG_E_ARG, "null argument");
+  TG_TRY(check_cg_params(cp));
+  tg_cg_result r{};
+  TG_TRY(solve_dev(L, *cp, (const double2*)b_dev, (double2*)x_dev, &r));
+  if (res) *res = r;
+  return solver_status(r.status);
+}
+
+int tg_gauge_action(tg_lattice* L, double* S) {
+  if (!L || !S) return fail(TG_E_ARG, "null argument");
+  gauge_action(L->stream, L->V, L->A, kNf / L->P.g, &L->ts->Sg0, L->red);
+  TG_CK(cudaGetLastError());
+  TG_CK(cudaMemcpyAsync(S, &L->ts->Sg0, sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  return TG_OK;
+}
+
+int tg_pseudofermion_action(tg_lattice* L, const tg_cg_params* cp, const double* phi, double* S,
+                            tg_cg_result* res) {
+  if (!L || !phi || !S) return fail(TG_E_ARG, "null argument");
+  TG_TRY(check_cg_params(cp));
+  TG_TRY(upload(L, L->vin, phi, 2 * (size_t)L->V));
+  tg_cg_result r{};
+  TG_TRY(solve_dev(L, *cp, L->vin, L->vout, &r));
+  if (res) *res = r;
+  redot(L->stream, L->V, L->vin, L->vout, &L->ts->Spf1, 0, L->red);
+  TG_CK(cudaGetLastError());
+  TG_CK(cudaMemcpyAsync(S, &L->ts->Spf1, sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  return solver_status(r.status);
+}
+
+int tg_md_action(tg_lattice* L, const double* n, double* S) {
+  if (!L || !n || !S) return fail(TG_E_ARG, "null argument");
+  TG_TRY(upload(L, L->vin, n, 2 * (size_t)L->V));
+  md_action(L->stream, L->g, op_k(L, 1), L->vin, L->Wt, L->Wx, &L->ts->Smd0, L->red);
+  TG_CK(cudaGetLastError());
+  TG_CK(cudaMemcpyAsync(S, &L->ts->Smd0, sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  return TG_OK;
+}
+
+int tg_force(tg_lattice* L, int npf, const double* chi, const double* noise, double* F) {
+  if (!L || !F || npf < 0 || (npf > 0 && !chi)) return fail(TG_E_ARG, "bad argument");
+  const size_t V = (size_t)L->V;
+  const double ep = exp(L->P.mu), em = exp(-L->P.mu);
+  TG_CK(cudaMemsetAsync(L->vout, 0, V * sizeof(double2), L->stream));  // F accumulates in vout
+  if (noise) TG_TRY(upload(L, L->noise, noise, 2 * V));
+  if (npf == 0)
+    force_field(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->vout, kNf / L->P.g,
+                1 | (noise ? 2 : 0));
+  for (int k = 0; k < npf; k++) {
+    TG_TRY(upload(L, L->chi, chi + 2 * V * k, 2 * V));
+    dslash64(L->stream, L->g, op_k(L, 0), L->chi, L->Mchi, L->Wt, L->Wx);
+    int flags = (k == 0 ? 1 : 0) | ((k == npf - 1 && noise) ? 2 : 0);
+    force_field(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->vout, kNf / L->P.g,
+                flags);
+  }
+  TG_CK(cudaGetLastError());
+  return download(L, F, L->vout, 2 * V);
+}
+
+int tg_momentum_step(tg_lattice* L, const tg_cg_params* cp, double* mom, int npf, const double* phi,
+                     const double* noise, double eps, tg_cg_result* res) {
+  if (!L || !mom || npf < 0 || npf > kMaxPf || (npf > 0 && !phi)) return fail(TG_E_ARG, "bad argument");
+  TG_TRY(check_cg_params(cp));
+  const size_t V = (size_t)L->V;
+  TG_TRY(ensure_pf(L, npf > 0 ? npf : 1));
+  const double ep = exp(L->P.mu), em = exp(-L->P.mu);
+  const double gfac = eps * kNf / L->P.g;
+  TG_TRY(upload(L, L->mom, mom, 2 * V));
+  if (noise) TG_TRY(upload(L, L->noise, noise, 2 * V));
+  if (npf > 0) TG_TRY(upload(L, L->phi, phi, 2 * V * npf));
+  tg_cg_result acc{};
+  if (npf == 0)
+    momentum_update(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->mom, eps, gfac,
+                    1 | (noise ? 2 : 0));
+  for (int k = 0; k < npf; k++) {
+    tg_cg_result r{};
+    TG_TRY(solve_dev(L, *cp, L->phi + V * k, L->chi, &r));
+    acc.iterations += r.iterations;
+    acc.reliable_updates += r.reliable_updates;
+    if (r.status > acc.status) acc.status = r.status;
+    acc.rr = r.rr;
+    acc.rr0 = r.rr0;
+    dslash64(L->stream, L->g, op_k(L, 0), L->chi, L->Mchi, L->Wt, L->Wx);
+    int flags = (k == 0 ? 1 : 0) | ((k == npf - 1 && noise) ? 2 : 0);
+    momentum_update(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->mom, eps, gfac,
+                    flags);
+  }
+  TG_CK(cudaGetLastError());
+  if (res) *res = acc;
+  TG_TRY(download(L, mom, L->mom, 2 * V));
+  return solver_status(acc.status);
+}
+
+int tg_gauge_step(tg_lattice* L, const double* mom, double eps) {
+  if (!L || !mom) return fail(TG_E_ARG, "null argument");
+  TG_TRY(upload(L, L->mom, mom, 2 * (size_t)L->V));
+  gauge_step(L->stream, L->g, L->P.bc_t, L->P.bc_x, L->A, L->mom, 2.0 * eps, 1, L->Wt, L->Wx, L->Wt32, L->Wx32);
+  TG_CK(cudaGetLastError());
+  TG_CK(cudaStreamSynchronize(L->stream));
+  return TG_OK;
+}
+
+int tg_mt_seed(tg_lattice* L, long seed, long warmup) {
+  if (!L || warmup < 0) return fail(TG_E_ARG, "bad argument");
+  L->mt.seed(seed);
+  for (long i = 0; i < warmup; i++) L->mt.next();
+  L->mt_seeded = true;
+  return TG_OK;
+}
+
+int tg_mt_uniforms(tg_lattice* L, double* out, long n) {
+  if (!L || (!out && n > 0) || n < 0) return fail(TG_E_ARG, "bad argument");
+  for (long i = 0; i < n; i++) out[i] = L->mt.next();
+  return TG_OK;
+}
+
+int tg_puregauge_sweeps(tg_lattice* L, int sweeps) {
+  if (!L || sweeps < 0) return fail(TG_E_ARG, "bad argument");
+  std::vector<double> A(2 * (size_t)L->V);
+  TG_TRY(download(L, A.data(), L->A, A.size()));
+  const double c = kNf / L->P.g;
+  for (int sw = 0; sw < sweeps; sw++)
+    for (size_t k = 0; k < A.size(); k++) {  // update_puregauge_hb, hmc.c:82-93
+      double s1 = -c * cos(A[k]);
+      double a = 2 * M_PI * L->mt.next() - M_PI;
+      double s2 = -c * cos(a);
+      if (L->mt.next() < exp(-s2 + s1)) A[k] = a;
+    }
+  return tg_set_gauge(L, A.data());
+}
+
+int tg_trajectory(tg_lattice* L, const tg_hmc_params* p, tg_traj_result* r) {
+  if (!L) return fail(TG_E_ARG, "null lattice");
+  TG_TRY(check_hmc_params(p));
+  if (p->rng == TG_RNG_PHILOX) return run_trajectory(L, *p, r);
+  if (p->rng != TG_RNG_MT) return fail(TG_E_ARG, "tg_trajectory needs TG_RNG_MT or TG_RNG_PHILOX");
+  // the reference's order: pseudofermion pairs, momentum pairs, noise pairs
+  // (hmc.c:695-698), then the accept uniform (hmc.c:738)
+  const size_t V = (size_t)L->V;
+  TG_TRY(ensure_pf(L, p->npf > 0 ? p->npf : 1));
+  double* h = L->h_stage;
+  size_t off = 0;
+  size_t n_eta = 2 * V * p->npf;
+  L->mt.gauss_pairs((long)V * p->npf, h);
+  off += n_eta;
+  L->mt.gauss_pairs((long)V, h + off);
+  off += 2 * V;
+  if (p->stochastic_term) L->mt.gauss_pairs((long)V, h + off);
+  double u = L->mt.next();
+  if (n_eta) TG_CK(cudaMemcpyAsync(L->eta, h, n_eta * sizeof(double), cudaMemcpyHostToDevice, L->stream));
+  TG_CK(cudaMemcpyAsync(L->mom, h + n_eta, 2 * V * sizeof(double), cudaMemcpyHostToDevice, L->stream));
+  if (p->stochastic_term)
+    TG_CK(cudaMemcpyAsync(L->noise, h + n_eta + 2 * V, 2 * V * sizeof(double), cudaMemcpyHostToDevice, L->stream));
+  L->h_ts->u = u;
+  TG_CK(cudaMemcpyAsync(&L->ts->u, &L->h_ts->u, sizeof(double), cudaMemcpyHostToDevice, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  return run_trajectory(L, *p, r);
+}
+
+int tg_trajectory_ext(tg_lattice* L, const tg_hmc_params* p, const double* eta, const double* mom,
+                      const double* noise, double u_accept, tg_traj_result* r) {
+  if (!L || !mom || (p && p->npf > 0 && !eta) || (p && p->stochastic_term && !noise))
+    return fail(TG_E_ARG, "null argument");
+  TG_TRY(check_hmc_params(p));
+  const size_t V = (size_t)L->V;
+  TG_TRY(ensure_pf(L, p->npf > 0 ? p->npf : 1));
+  if (p->npf > 0) TG_TRY(upload(L, L->eta, eta, 2 * V * p->npf));
+  TG_TRY(upload(L, L->mom, mom, 2 * V));
+  if (p->stochastic_term) TG_TRY(upload(L, L->noise, noise, 2 * V));
+  L->h_ts->u = u_accept;
+  TG_CK(cudaMemcpyAsync(&L->ts->u, &L->h_ts->u, sizeof(double), cudaMemcpyHostToDevice, L->stream));
+  tg_hmc_params q = *p;
+  q.rng = TG_RNG_EXTERNAL;
+  return run_trajectory(L, q, r);
+}
+
+}  // extern "C"

@@ -1,0 +1,163 @@
+// tg_internal.cuh -- shared device/host definitions of the Thirring2D GB300 library.
+//
+// Layout in HBM (one lattice, V = nt*nx sites, site s = t*nx + x, t-major as
+// in the reference hmc.c loops):
+//   gauge field A        double2[V]   (.x = A_t, .y = A_x)   hmc.c A[t][x][dir]
+//   momenta              double2[V]   (.x = p_t, .y = p_x)
+//   fermion vectors      double2[V] / float2[V]  (re, im)    hmc.c v[t][x]
+//   link coefficients    Wt[V], Wx[V] (complex, FP64 and FP32 copies)
+//                        W_mu(s) = 0.5 * eta_mu(s) * bc_mu(s) * exp(i A_mu(s))
+//                        i.e. every real factor of a hop in hmc.c:140-180
+//                        except exp(+-mu) is folded in once per gauge update.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/thirring_gpu.h"
+
+namespace tg {
+
+constexpr int kBlock = 256;        // threads per block for site kernels
+constexpr int kNf = 2;             // flavours in the gauge action, hmc.c:28
+
+template <typename R> struct C2T;
+template <> struct C2T<double> { using type = double2; };
+template <> struct C2T<float> { using type = float2; };
+template <typename R> using C2 = typename C2T<R>::type;
+
+template <typename R> __host__ __device__ __forceinline__ C2<R> mk(R a, R b) { C2<R> v; v.x = a; v.y = b; return v; }
+
+// acc += w * v
+template <typename R> __device__ __forceinline__ void cmac(C2<R>& acc, C2<R> w, C2<R> v) {
+  acc.x = fma(w.x, v.x, acc.x); acc.x = fma(-w.y, v.y, acc.x);
+  acc.y = fma(w.x, v.y, acc.y); acc.y = fma(w.y, v.x, acc.y);
+}
+// acc -= conj(w) * v
+template <typename R> __device__ __forceinline__ void cmsc(C2<R>& acc, C2<R> w, C2<R> v) {
+  acc.x = fma(-w.x, v.x, acc.x); acc.x = fma(-w.y, v.y, acc.x);
+  acc.y = fma(-w.x, v.y, acc.y); acc.y = fma(w.y, v.x, acc.y);
+}
+// w * v
+template <typename R> __device__ __forceinline__ C2<R> cmul(C2<R> w, C2<R> v) {
+  return mk<R>(fma(w.x, v.x, -w.y * v.y), fma(w.x, v.y, w.y * v.x));
+}
+// conj(w) * v
+template <typename R> __device__ __forceinline__ C2<R> cjmul(C2<R> w, C2<R> v) {
+  return mk<R>(fma(w.x, v.x, w.y * v.y), fma(w.x, v.y, -w.y * v.x));
+}
+
+// Lattice geometry for kernels (by value).
+struct Geo {
+  int nt, nx, V;
+  float inv_nx;   // for the division-free site -> (t, x) split
+};
+
+__device__ __forceinline__ void site_tx(const Geo& g, int s, int& t, int& x) {
+  // V < 2^24 keeps float(s) exact; the fix-up absorbs the rounding of s/nx.
+  t = __float2int_rz(__int2float_rn(s) * g.inv_nx);
+  x = s - t * g.nx;
+  if (x < 0) { t -= 1; x += g.nx; } else if (x >= g.nx) { t += 1; x -= g.nx; }
+}
+
+struct Nbr { int tp, tm, xp, xm; };
+__device__ __forceinline__ Nbr neighbours(const Geo& g, int s, int t, int x) {
+  Nbr n;
+  n.tp = (t == g.nt - 1) ? s + g.nx - g.V : s + g.nx;
+  n.tm = (t == 0) ? s - g.nx + g.V : s - g.nx;
+  n.xp = (x == g.nx - 1) ? s - (g.nx - 1) : s + 1;
+  n.xm = (x == 0) ? s + (g.nx - 1) : s - 1;
+  return n;
+}
+
+// Operator constants for M (dag = 0) or the true adjoint M^dagger (dag = 1):
+//   out = m in + cf*Wt in(s+t) + cb*conj(Wt(s-t)) in(s-t) + cx*(Wx in(s+x) - conj(Wx(s-x)) in(s-x))
+// M: cf = e^mu, cb = -e^-mu, cx = +1 (hmc.c:137-180); M^dag: cf = -e^-mu, cb = e^mu, cx = -1.
+template <typename R> struct OpK {
+  R m, cf, cb, cx;
+};
+
+// ---------------------------------------------------------------------------
+// Block reduction (deterministic: fixed shuffle tree, then fixed smem order)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int BS> __device__ __forceinline__ double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0;
+  if (w == 0) {
+    r = (lane < BS / 32) ? sh[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+
+// Grid-wide deterministic sum with the "last block finishes" pattern: every
+// block stores its partial, the block that arrives last adds the partials in
+// index order.  Returns true in exactly one block (all its threads), with the
+// total in *total (thread 0 of that block).  `counter` must be 0 on entry
+// and is 0 again on exit.
+template <int BS>
+__device__ __forceinline__ bool grid_sum(double v, double* partials, unsigned* counter, double* total) {
+  __shared__ double sh[BS / 32];
+  __shared__ bool is_last;
+  double b = block_sum<BS>(v, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b;
+    __threadfence();
+    unsigned prev = atomicAdd(counter, 1u);
+    is_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  __threadfence();
+  double s = 0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += BS) s += __ldcg(partials + i);
+  s = block_sum<BS>(s, sh);
+  if (threadIdx.x == 0) {
+    *total = s;
+    *counter = 0u;
+  }
+  return true;
+}
+
+inline int nblocks(int n, int bs = kBlock) { return (n + bs - 1) / bs; }
+
+// ---------------------------------------------------------------------------
+// Device state of one CG solve.  Lives in device memory; all the scalar
+// recurrences of CG run on the device so no iteration needs the host.
+// ---------------------------------------------------------------------------
+struct CgState {
+  double rr;        // |r|^2 of the (recursive) residual
+  double rr0;       // |b|^2
+  double stop;      // stop when rr < stop
+  double alpha, beta;
+  double rr_true;   // |b - A x|^2 at the last reliable update (mixed)
+  int iter, maxiter, status, done;
+  int since_ru, ru_interval, n_ru, need_ru;
+  int log_index;    // slot of the per-trajectory solve log, -1 for none
+  int pad_;
+};
+
+// Per-solve record kept for the host (iterations, status, reliable updates).
+struct CgLog {
+  int iter, status, n_ru, pad_;
+  double rr, rr0;
+};
+
+// Graph conditional handles a CG kernel may set; use == 0 outside graphs.
+struct Cond {
+  cudaGraphConditionalHandle loop;   // WHILE node of the solve
+  cudaGraphConditionalHandle ru;     // IF node of the reliable update (mixed)
+  int use;
+};
+
+}  // namespace tg

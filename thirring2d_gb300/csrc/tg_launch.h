@@ -1,0 +1,86 @@
+// tg_launch.h -- host-side launch interface between tg_kernels.cu and tg_capi.cu.
+#pragma once
+
+#include "tg_internal.cuh"
+
+namespace tg {
+
+// Per-trajectory scalars on the device (filled by the reduction kernels).
+struct TrajStats {
+  double Sg0, Spf0, Smd0, Smom0;
+  double Sg1, Spf1, Smd1, Smom1;
+  double dH, u;
+  int accepted, pad_;
+  unsigned long long traj;   // Philox trajectory counter
+};
+
+struct CgBufs64 {          // FP64 CG work vectors
+  double2 *r, *p, *Mp;
+};
+struct CgBufsMixed {       // FP32 CG work vectors + FP64 accumulators
+  float2 *xs, *rs, *ps, *Mps;
+  double2* tmp64;          // M x for the reliable update
+};
+
+struct Red {               // reduction scratch
+  double* partials;
+  unsigned* counter;
+};
+
+struct Links {
+  const double2 *Wt, *Wx;
+  const float2 *Wt32, *Wx32;
+};
+
+// link coefficients of A (both precisions)
+void link_phase(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,
+                float2* Wt32, float2* Wx32);
+// A += c*mom, nadd times in sequence, then link coefficients
+void gauge_step(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double2* A, const double2* mom, double c,
+                int nadd, double2* Wt, double2* Wx, float2* Wt32, float2* Wx32);
+void dslash64(cudaStream_t s, const Geo& g, const OpK<double>& k, const double2* in, double2* out,
+              const double2* Wt, const double2* Wx);
+void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, const float2* in, float2* out, const float2* Wt,
+              const float2* Wx);
+
+// CG on M^dag M (FP64).  km = M constants, kd = M^dag constants.
+void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
+               const Red& red, double rel_tol, double abs_tol2, int maxiter, int log_index, Cond c);
+void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
+               double2* x, const CgBufs64& w, CgState* st, CgLog* log, const Red& red, Cond c);
+// Mixed precision: FP32 iterations + FP64 reliable update
+void cgmx_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufsMixed& w, CgState* st,
+               const Red& red, double rel_tol, double abs_tol2, int maxiter, int ru_interval, int log_index,
+               Cond c);
+void cgmx_iter(cudaStream_t s, const Geo& g, const OpK<float>& km, const OpK<float>& kd, const Links& L,
+               const CgBufsMixed& w, CgState* st, const Red& red, Cond c);
+void cgmx_reliable(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
+                   const double2* b, double2* x, const CgBufsMixed& w, CgState* st, CgLog* log, const Red& red,
+                   Cond c);
+
+// reductions into a device double (accumulate: *dst += sum, else *dst = sum)
+void norm2(cudaStream_t s, int n, const double2* v, double* dst, int accumulate, const Red& red);
+void redot(cudaStream_t s, int n, const double2* u, const double2* v, double* dst, int accumulate, const Red& red);
+void gauge_action(cudaStream_t s, int n, const double2* A, double fac, double* dst, const Red& red);
+void md_action(cudaStream_t s, const Geo& g, const OpK<double>& kd, const double2* nz, const double2* Wt,
+               const double2* Wx, double* dst, const Red& red);
+
+// mom -= eps*F; flags bit0: gauge force first (gfac = eps*Nf/g), bit1: stochastic-term force last
+void momentum_update(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
+                     const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise,
+                     double2* mom, double eps, double gfac, int flags);
+// F = dS/dA (for tests): same pieces, written instead of applied
+void force_field(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
+                 const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise, double2* F,
+                 double gfac, int flags);
+
+// Philox Gaussian fields: out[n] complex pairs for (seed, stats->traj, stream_id)
+void philox_gauss(cudaStream_t s, int n, unsigned long long seed, const TrajStats* ts, unsigned stream_id,
+                  double2* out);
+void philox_uniform(cudaStream_t s, unsigned long long seed, TrajStats* ts, unsigned stream_id);
+
+void finish_trajectory(cudaStream_t s, TrajStats* ts);
+void accept_copy(cudaStream_t s, int n, const TrajStats* ts, double2* A, const double2* Anew);
+void puregauge_dummy();
+
+}  // namespace tg
