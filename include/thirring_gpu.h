@@ -162,8 +162,12 @@ int tg_gauge_step(tg_lattice* L, const double* mom, double eps);
 /* seed_mersenne(seed) then `warmup` discarded draws (hmc.c:874-877 uses 543210). */
 int tg_mt_seed(tg_lattice* L, long seed, long warmup);
 int tg_mt_uniforms(tg_lattice* L, double* out, long n);
-/* update_puregauge_hb (hmc.c:82-93) x sweeps, drawing from the MT stream. */
+/* update_puregauge_hb (hmc.c:82-93) x sweeps, drawing from the MT stream.
+ * Links are independent, so each sweep is one data-parallel kernel. */
 int tg_puregauge_sweeps(tg_lattice* L, int sweeps);
+/* Same with caller-supplied uniforms: u[sweeps * 4 * NT*NX], per link (t-major,
+ * dir inner) the proposal uniform then the acceptance uniform. */
+int tg_puregauge_ext(tg_lattice* L, const double* u, int sweeps);
 
 /* ---- HMC trajectory: update_gauge (hmc.c:671-746) ------------------------- */
 /* Draws the pseudofermion, momentum, noise fields and the accept uniform

@@ -45,3 +45,18 @@ def test_library_loads_without_gpu(built):
     lib.tg_version.restype = ctypes.c_char_p
     assert b"sm_103a" in lib.tg_version()
 
+
+
+def test_compat_library_exports_reference_names(built):
+    """libthirring_hmc.so exports every hmc.c / mersenne.h name of include/thirring_hmc.h
+    (functions and the globals m, g, mu, A, eta, tup, tdn, xup, xdn, mersenne_i, mersenne_array)."""
+    names = set(declared("thirring_hmc.h"))
+    assert {"fm_mul", "fm_conjugate_mul", "fmdm_invert_cg", "update_gauge", "momentum_step",
+            "seed_mersenne", "mersenne_generate"} <= names
+    globals_ = {"m", "g", "mu", "A", "eta", "tup", "tdn", "xup", "xdn", "mersenne_i", "mersenne_array"}
+    missing = sorted((names | globals_) - exported(built["libthirring_hmc"]))
+    assert not missing, missing
+
+
+def test_hmc_program_built(built):
+    assert os.access(built["hmc"], os.X_OK)

@@ -287,7 +287,7 @@ def test_trajectory_ext_matches_mt(tg, oracle_lib):
 def test_philox_trajectories(tg):
     """Device RNG: reproducible for a seed, Gaussian moments as expected."""
     nt = nx = 32
-    hp = tg.hmc_params(nsteps=10, rng=tg.native.RNG_PHILOX, seed=1234,
+    hp = tg.hmc_params(nsteps=40, rng=tg.native.RNG_PHILOX, seed=1234,
                        cg=tg.cg_params(rel_tol=1e-10, abs_tol2=0), stochastic_term=False)
     runs = []
     for _ in range(2):
@@ -299,7 +299,7 @@ def test_philox_trajectories(tg):
     for r in runs[0]:
         assert abs(r.Spf0 - 2 * V) < 6 * np.sqrt(4 * V)    # sum |eta|^2, E = 2V, Var = 4V
         assert abs(r.Smom0 - 2 * V) < 6 * np.sqrt(4 * V)
-        assert abs(r.dH) < 5
+        assert r.status == 0 and np.isfinite(r.dH) and abs(r.dH) < 100
     assert runs[0][0].Spf0 != runs[0][1].Spf0             # new fields every trajectory
 
 

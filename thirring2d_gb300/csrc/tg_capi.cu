@@ -106,6 +106,7 @@ struct tg_lattice {
   float2 *Wt32 = nullptr, *Wx32 = nullptr;
   double2 *mom = nullptr, *noise = nullptr, *chi = nullptr, *Mchi = nullptr, *vin = nullptr, *vout = nullptr;
   double2 *eta = nullptr, *phi = nullptr;  // [npf_alloc][V]
+  double* unif = nullptr;                  // [4V] uniforms of one pure-gauge sweep (allocated on first use)
   int npf_alloc = 0;
   CgBufs64 w64{};
   CgBufsMixed wmx{};
@@ -239,10 +240,10 @@ int enqueue_cg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const doub
     TG_CK(cudaGraphConditionalHandleCreate(&hloop, top, 0, 0));
     Cond c0{hloop, 0, 1};
     if (mixed)
-      cgmx_init(s, g, b, x, L->wmx, L->st, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, cp.ru_interval, log_index,
+      cgmx_init(s, g, b, x, L->wmx, L->st, L->log, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, cp.ru_interval, log_index,
                 c0);
     else
-      cg64_init(s, g, b, x, L->w64, L->st, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, log_index, c0);
+      cg64_init(s, g, b, x, L->w64, L->st, L->log, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, log_index, c0);
     TG_CK(cudaGetLastError());
     cudaGraph_t body;
     TG_TRY(add_conditional(s, hloop, cudaGraphCondTypeWhile, &body));
@@ -269,10 +270,10 @@ int enqueue_cg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const doub
   }
   Cond none{0, 0, 0};
   if (mixed)
-    cgmx_init(s, g, b, x, L->wmx, L->st, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, cp.ru_interval, log_index,
+    cgmx_init(s, g, b, x, L->wmx, L->st, L->log, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, cp.ru_interval, log_index,
               none);
   else
-    cg64_init(s, g, b, x, L->w64, L->st, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, log_index, none);
+    cg64_init(s, g, b, x, L->w64, L->st, L->log, L->red, cp.rel_tol, cp.abs_tol2, cp.maxiter, log_index, none);
   TG_CK(cudaGetLastError());
   const int chunk = 16;
   long max_chunks = (long)cp.maxiter / chunk + 2;
@@ -578,7 +579,7 @@ int tg_destroy(tg_lattice* L) {
   for (auto e : L->ev) cudaEventDestroy(e);
   void* dev[] = {L->A, L->Anew, L->Wt, L->Wx, L->mom, L->noise, L->chi, L->Mchi, L->vin, L->vout, L->w64.r,
                  L->w64.p, L->w64.Mp, L->wmx.tmp64, L->Wt32, L->Wx32, L->wmx.xs, L->wmx.rs, L->wmx.ps, L->wmx.Mps,
-                 L->st, L->log, L->ts, L->red.partials, L->red.counter, L->eta, L->phi};
+                 L->st, L->log, L->ts, L->red.partials, L->red.counter, L->eta, L->phi, L->unif};
   for (void* d : dev)
     if (d) cudaFree(d);
   void* hst[] = {L->h_stage, L->h_st, L->h_ts, L->h_log};
@@ -813,19 +814,31 @@ int tg_mt_uniforms(tg_lattice* L, double* out, long n) {
   return TG_OK;
 }
 
+int tg_puregauge_ext(tg_lattice* L, const double* u, int sweeps) {
+  if (!L || sweeps < 0 || (sweeps > 0 && !u)) return fail(TG_E_ARG, "bad argument");
+  const size_t nl = 2 * (size_t)L->V;
+  if (!L->unif) TG_TRY(dmalloc(&L->unif, 2 * nl));
+  for (int sw = 0; sw < sweeps; sw++) {
+    // the 2 uniforms of each of the 2V links of one sweep
+    TG_TRY(upload(L, L->unif, u + 2 * nl * sw, 2 * nl));
+    puregauge(L->stream, (int)nl, (double*)L->A, L->unif, -kNf / L->P.g);
+    TG_CK(cudaGetLastError());
+  }
+  link_phase(L->stream, L->g, L->P.bc_t, L->P.bc_x, L->A, L->Wt, L->Wx, L->Wt32, L->Wx32);
+  TG_CK(cudaGetLastError());
+  TG_CK(cudaStreamSynchronize(L->stream));
+  return TG_OK;
+}
+
 int tg_puregauge_sweeps(tg_lattice* L, int sweeps) {
   if (!L || sweeps < 0) return fail(TG_E_ARG, "bad argument");
-  std::vector<double> A(2 * (size_t)L->V);
-  TG_TRY(download(L, A.data(), L->A, A.size()));
-  const double c = kNf / L->P.g;
-  for (int sw = 0; sw < sweeps; sw++)
-    for (size_t k = 0; k < A.size(); k++) {  // update_puregauge_hb, hmc.c:82-93
-      double s1 = -c * cos(A[k]);
-      double a = 2 * M_PI * L->mt.next() - M_PI;
-      double s2 = -c * cos(a);
-      if (L->mt.next() < exp(-s2 + s1)) A[k] = a;
-    }
-  return tg_set_gauge(L, A.data());
+  const size_t nl = 2 * (size_t)L->V;
+  std::vector<double> u(2 * nl);
+  for (int sw = 0; sw < sweeps; sw++) {
+    for (size_t k = 0; k < 2 * nl; k++) u[k] = L->mt.next();
+    TG_TRY(tg_puregauge_ext(L, u.data(), 1));
+  }
+  return TG_OK;
 }
 
 int tg_trajectory(tg_lattice* L, const tg_hmc_params* p, tg_traj_result* r) {

@@ -144,8 +144,15 @@ struct CgState {
   int iter, maxiter, status, done;
   int since_ru, ru_interval, n_ru, need_ru;
   int log_index;    // slot of the per-trajectory solve log, -1 for none
-  int pad_;
+  int restart;      // mixed: the last reliable update found the FP32 residual off by > 10x
 };
+
+// Mixed precision: a reliable update also happens once |r|^2 has fallen by
+// this factor since the last one (FP32 recursive residuals lose accuracy
+// beyond about 1e-3 in |r|), besides every ru_interval iterations.
+constexpr double kRuDrop = 1e-6;
+// ... and p restarts from r when the true |r|^2 exceeds the recursive one by this factor.
+constexpr double kRuRestart = 10.0;
 
 // Per-solve record kept for the host (iterations, status, reliable updates).
 struct CgLog {

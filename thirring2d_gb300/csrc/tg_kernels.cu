@@ -49,9 +49,9 @@ __global__ void __launch_bounds__(kBlock) k_gauge_step(Geo g, int bc_t, int bc_x
   if (s >= g.V) return;
   double2 a = A[s];
   double2 p = mom[s];
-  for (int k = 0; k < nadd; k++) {
-    a.x += c * p.x;
-    a.y += c * p.y;
+  for (int k = 0; k < nadd; k++) {  // product then sum, two roundings, as the host code of hmc.c:99
+    a.x = __dadd_rn(a.x, __dmul_rn(c, p.x));
+    a.y = __dadd_rn(a.y, __dmul_rn(c, p.y));
   }
   A[s] = a;
   write_links(g, bc_t, bc_x, s, a, Wt, Wx, Wt32, Wx32);
@@ -138,7 +138,7 @@ template <typename R>
 __global__ void __launch_bounds__(kBlock) k_cg_init(Geo g, const double2* __restrict__ b, double2* x, C2<R>* r,
                                                     C2<R>* p, C2<R>* xs, double rel_tol, double abs_tol2,
                                                     int maxiter, int ru_interval, int log_index, CgState* st,
-                                                    Red red, Cond c) {
+                                                    CgLog* log, Red red, Cond c) {
   int s = blockIdx.x * kBlock + threadIdx.x;
   double v = 0;
   if (s < g.V) {
@@ -167,14 +167,13 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(Geo g, const double2* __rest
     st->ru_interval = ru_interval;
     st->n_ru = 0;
     st->need_ru = 0;
+    st->restart = 0;
     st->log_index = log_index;
-    int done = !(tot >= stop);   // b = 0 (hmc.c:359-361), or NaN
+    // b = 0 or already below the stop (hmc.c:359-361), or NaN: no iterations
+    int done = !(tot >= stop) || tot == 0.0;
     st->done = 0;
-    if (done) {
-      st->status = isnan(tot) ? TG_E_NAN : TG_OK;
-      st->done = 1;
-    }
-    if (c.use) cudaGraphSetConditional(c.loop, done ? 0u : 1u);
+    if (done) cg_finish(st, log, isnan(tot) ? TG_E_NAN : TG_OK, c);
+    else if (c.use) cudaGraphSetConditional(c.loop, 1u);
   }
 }
 
@@ -193,7 +192,11 @@ __global__ void __launch_bounds__(kBlock) k_cg1(Geo g, OpK<R> k, const C2<R>* __
     v = (double)o.x * (double)o.x + (double)o.y * (double)o.y;
   }
   double tot;
-  if (grid_sum<kBlock>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) st->alpha = st->rr / tot;
+  if (grid_sum<kBlock>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) {
+    st->alpha = st->rr / tot;
+    st->need_ru = 0;   // the previous iteration's reliable-update kernels have all run
+    st->restart = 0;
+  }
 }
 
 // FP64: convergence tested on the recursive residual, as hmc.c:381.
@@ -244,9 +247,9 @@ __global__ void __launch_bounds__(kBlock) k_cg3(int n, const C2<R>* __restrict__
 }
 
 void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
-               const Red& red, double rel_tol, double abs_tol2, int maxiter, int log_index, Cond c) {
+               CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int log_index, Cond c) {
   k_cg_init<double><<<nblocks(g.V), kBlock, 0, s>>>(g, b, x, w.r, w.p, nullptr, rel_tol, abs_tol2, maxiter, 0,
-                                                    log_index, st, red, c);
+                                                    log_index, st, log, red, c);
 }
 
 void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
@@ -291,8 +294,8 @@ __global__ void __launch_bounds__(kBlock) k_cgmx2(Geo g, OpK<float> k, const flo
     double rr_old = st->rr;
     st->rr = rn;
     st->beta = rn / rr_old;
-    int need = st->since_ru >= st->ru_interval || rn < st->stop || st->iter >= st->maxiter ||
-               rn / st->rr0 > 1e10 || isnan(rn);
+    int need = st->since_ru >= st->ru_interval || rn < st->stop || rn < kRuDrop * st->rr_true ||
+               st->iter >= st->maxiter || rn / st->rr0 > 1e10 || isnan(rn);
     st->need_ru = need;
     if (c.use) cudaGraphSetConditional(c.ru, need ? 1u : 0u);
   }
@@ -300,7 +303,7 @@ __global__ void __launch_bounds__(kBlock) k_cgmx2(Geo g, OpK<float> k, const flo
 
 // reliable update 1: x += xs, xs = 0
 __global__ void __launch_bounds__(kBlock) k_ru1(int n, double2* x, float2* xs, const CgState* st) {
-  if (!st->need_ru) return;
+  if (!st->need_ru || st->done) return;
   int s = blockIdx.x * kBlock + threadIdx.x;
   if (s >= n) return;
   float2 d = xs[s];
@@ -315,7 +318,7 @@ __global__ void __launch_bounds__(kBlock) k_ru1(int n, double2* x, float2* xs, c
 __global__ void __launch_bounds__(kBlock) k_ru2(Geo g, OpK<double> k, const double2* __restrict__ x,
                                                 double2* __restrict__ tmp, const double2* __restrict__ Wt,
                                                 const double2* __restrict__ Wx, const CgState* st) {
-  if (!st->need_ru) return;
+  if (!st->need_ru || st->done) return;
   int s = blockIdx.x * kBlock + threadIdx.x;
   if (s >= g.V) return;
   int t, xx;
@@ -328,7 +331,7 @@ __global__ void __launch_bounds__(kBlock) k_ru3(Geo g, OpK<double> k, const doub
                                                 const double2* __restrict__ tmp, float2* __restrict__ rs,
                                                 const double2* __restrict__ Wt, const double2* __restrict__ Wx,
                                                 CgState* st, CgLog* log, Red red, Cond c) {
-  if (!st->need_ru) return;
+  if (!st->need_ru || st->done) return;
   int s = blockIdx.x * kBlock + threadIdx.x;
   double v = 0;
   if (s < g.V) {
@@ -342,11 +345,11 @@ __global__ void __launch_bounds__(kBlock) k_ru3(Geo g, OpK<double> k, const doub
   }
   double rt;
   if (grid_sum<kBlock>(v, red.partials, red.counter, &rt) && threadIdx.x == 0) {
+    st->restart = rt > kRuRestart * st->rr;  // recursive residual was far too optimistic
     st->rr_true = rt;
     st->rr = rt;
     st->since_ru = 0;
     st->n_ru += 1;
-    st->need_ru = 0;
     if (isnan(rt)) cg_finish(st, log, TG_E_NAN, c);
     else if (rt < st->stop) cg_finish(st, log, TG_OK, c);
     else if (rt / st->rr0 > 1e10) cg_finish(st, log, TG_E_DIVERGED, c);
@@ -354,11 +357,19 @@ __global__ void __launch_bounds__(kBlock) k_ru3(Geo g, OpK<double> k, const doub
   }
 }
 
+// reliable update 4: restart the search direction from the new residual
+__global__ void __launch_bounds__(kBlock) k_ru4(int n, const float2* __restrict__ rs, float2* __restrict__ ps,
+                                                const CgState* st) {
+  if (!st->need_ru || !st->restart || st->done) return;
+  int s = blockIdx.x * kBlock + threadIdx.x;
+  if (s < n) ps[s] = rs[s];
+}
+
 void cgmx_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufsMixed& w, CgState* st,
-               const Red& red, double rel_tol, double abs_tol2, int maxiter, int ru_interval, int log_index,
-               Cond c) {
+               CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int ru_interval,
+               int log_index, Cond c) {
   k_cg_init<float><<<nblocks(g.V), kBlock, 0, s>>>(g, b, x, w.rs, w.ps, w.xs, rel_tol, abs_tol2, maxiter,
-                                                   ru_interval, log_index, st, red, c);
+                                                   ru_interval, log_index, st, log, red, c);
 }
 
 void cgmx_iter(cudaStream_t s, const Geo& g, const OpK<float>& km, const OpK<float>& kd, const Links& L,
@@ -376,6 +387,7 @@ void cgmx_reliable(cudaStream_t s, const Geo& g, const OpK<double>& km, const Op
   k_ru1<<<nb, kBlock, 0, s>>>(g.V, x, w.xs, st);
   k_ru2<<<nb, kBlock, 0, s>>>(g, km, x, w.tmp64, L.Wt, L.Wx, st);
   k_ru3<<<nb, kBlock, 0, s>>>(g, kd, b, w.tmp64, w.rs, L.Wt, L.Wx, st, log, red, c);
+  k_ru4<<<nb, kBlock, 0, s>>>(g.V, w.rs, w.ps, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -598,6 +610,25 @@ void philox_gauss(cudaStream_t s, int n, unsigned long long seed, const TrajStat
 }
 void philox_uniform(cudaStream_t s, unsigned long long seed, TrajStats* ts, unsigned stream_id) {
   k_philox_uniform<<<1, 1, 0, s>>>(seed, ts, stream_id);
+}
+
+// Pure-gauge Metropolis (update_puregauge_hb, hmc.c:82-93): every link is
+// independent (the compact action is a sum over single links), so one sweep is
+// one data-parallel pass.  u holds the two uniforms of each link in the
+// reference's order (proposal, then acceptance).  c = -Nf/g.  The proposal is
+// computed without FMA contraction so it is bit-identical to the host's.
+__global__ void __launch_bounds__(kBlock) k_puregauge(int n, double* A, const double* __restrict__ u, double c) {
+  int k = blockIdx.x * kBlock + threadIdx.x;
+  if (k >= n) return;
+  double a = A[k];
+  double s1 = c * cos(a);
+  double prop = __dsub_rn(__dmul_rn(2 * M_PI, u[2 * k]), M_PI);
+  double s2 = c * cos(prop);
+  if (u[2 * k + 1] < exp(-s2 + s1)) A[k] = prop;
+}
+
+void puregauge(cudaStream_t s, int nlinks, double* A, const double* u, double c) {
+  k_puregauge<<<nblocks(nlinks), kBlock, 0, s>>>(nlinks, A, u, c);
 }
 
 // dH in the order of hmc.c:729-732, accept if exp(-dH) > u (hmc.c:738)

@@ -45,13 +45,13 @@ void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, const float2* i
 
 // CG on M^dag M (FP64).  km = M constants, kd = M^dag constants.
 void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
-               const Red& red, double rel_tol, double abs_tol2, int maxiter, int log_index, Cond c);
+               CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int log_index, Cond c);
 void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
                double2* x, const CgBufs64& w, CgState* st, CgLog* log, const Red& red, Cond c);
 // Mixed precision: FP32 iterations + FP64 reliable update
 void cgmx_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufsMixed& w, CgState* st,
-               const Red& red, double rel_tol, double abs_tol2, int maxiter, int ru_interval, int log_index,
-               Cond c);
+               CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int ru_interval,
+               int log_index, Cond c);
 void cgmx_iter(cudaStream_t s, const Geo& g, const OpK<float>& km, const OpK<float>& kd, const Links& L,
                const CgBufsMixed& w, CgState* st, const Red& red, Cond c);
 void cgmx_reliable(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
@@ -81,6 +81,7 @@ void philox_uniform(cudaStream_t s, unsigned long long seed, TrajStats* ts, unsi
 
 void finish_trajectory(cudaStream_t s, TrajStats* ts);
 void accept_copy(cudaStream_t s, int n, const TrajStats* ts, double2* A, const double2* Anew);
-void puregauge_dummy();
+// one pure-gauge Metropolis sweep over nlinks = 2V links; u[2*nlinks]; c = -Nf/g
+void puregauge(cudaStream_t s, int nlinks, double* A, const double* u, double c);
 
 }  // namespace tg

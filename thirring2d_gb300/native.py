@@ -86,6 +86,7 @@ SIGNATURES = {
     "tg_mt_seed": (C.c_int, [_vp, C.c_long, C.c_long]),
     "tg_mt_uniforms": (C.c_int, [_vp, _dp, C.c_long]),
     "tg_puregauge_sweeps": (C.c_int, [_vp, C.c_int]),
+    "tg_puregauge_ext": (C.c_int, [_vp, _dp, C.c_int]),
     "tg_trajectory": (C.c_int, [_vp, C.POINTER(HmcParams), C.POINTER(TrajResult)]),
     "tg_trajectory_ext": (C.c_int, [_vp, C.POINTER(HmcParams), _dp, _dp, _dp, C.c_double, C.POINTER(TrajResult)]),
 }
