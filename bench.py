@@ -47,7 +47,7 @@ DSLASH_BYTES_PER_SITE = 64
 # CG iterations per trajectory of this workload (FP64 solver; sum over the 21
 # solves), measured by the GPU arm on GB300 and used to scale the reference's
 # per-iteration CPU time to a trajectory.
-CG_ITERS_PER_TRAJ = 8600
+CG_ITERS_PER_TRAJ = 7900
 L2_FLUSH_BYTES = 256 << 20
 
 

@@ -133,14 +133,15 @@ OpK<double> op_k(const tg_lattice* L, int dagger) {
   double ep = exp(L->P.mu), em = exp(-L->P.mu);
   OpK<double> k;
   k.m = L->P.m;
-  if (!dagger) { k.cf = ep; k.cb = -em; k.cx = 1.0; }
-  else { k.cf = -em; k.cb = ep; k.cx = -1.0; }
+  if (!dagger) { k.cf = ep; k.cb = -em; }
+  else { k.cf = -em; k.cb = ep; }
+  k.mu0 = L->P.mu == 0.0;
   return k;
 }
 OpK<float> op_k32(const tg_lattice* L, int dagger) {
   OpK<double> k = op_k(L, dagger);
   OpK<float> f;
-  f.m = (float)k.m; f.cf = (float)k.cf; f.cb = (float)k.cb; f.cx = (float)k.cx;
+  f.m = (float)k.m; f.cf = (float)k.cf; f.cb = (float)k.cb; f.mu0 = k.mu0;
   return f;
 }
 Links links(const tg_lattice* L) { return Links{L->Wt, L->Wx, L->Wt32, L->Wx32}; }
@@ -402,20 +403,20 @@ int enqueue_trajectory(tg_lattice* L, cudaStream_t s, const tg_hmc_params& p, bo
     return TG_OK;
   };
   if (p.rng == TG_RNG_PHILOX) {
-    for (int k = 0; k < p.npf; k++) philox_gauss(s, V, p.seed, ts, (unsigned)k, L->eta + (size_t)k * V);
-    philox_gauss(s, V, p.seed, ts, 16u, L->mom);
-    if (use_noise) philox_gauss(s, V, p.seed, ts, 17u, L->noise);
+    for (int k = 0; k < p.npf; k++) philox_gauss(s, g, p.seed, ts, (unsigned)k, L->eta + (size_t)k * V);
+    philox_gauss(s, g, p.seed, ts, 16u, L->mom);
+    if (use_noise) philox_gauss(s, g, p.seed, ts, 17u, L->noise);
     philox_uniform(s, p.seed, ts, 18u);
   }
   link_phase(s, g, L->P.bc_t, L->P.bc_x, L->A, L->Wt, L->Wx, L->Wt32, L->Wx32);
   // start: S_pf = |eta|^2 exactly (phi = M^dag eta), hmc.c:418-436
   TG_CK(cudaMemsetAsync(&ts->Spf0, 0, sizeof(double), s));
   for (int k = 0; k < p.npf; k++) {
-    norm2(s, V, L->eta + (size_t)k * V, &ts->Spf0, 1, L->red);
-    dslash64(s, g, kd, L->eta + (size_t)k * V, L->phi + (size_t)k * V, L->Wt, L->Wx);
+    norm2(s, g, L->eta + (size_t)k * V, &ts->Spf0, 1, L->red);
+    dslash64(s, g, kd, 1, L->eta + (size_t)k * V, L->phi + (size_t)k * V, L->Wt, L->Wx);
   }
-  norm2(s, V, L->mom, &ts->Smom0, 0, L->red);
-  gauge_action(s, V, L->A, kNf / L->P.g, &ts->Sg0, L->red);
+  norm2(s, g, L->mom, &ts->Smom0, 0, L->red);
+  gauge_action(s, g, L->A, kNf / L->P.g, &ts->Sg0, L->red);
   if (use_noise) md_action(s, g, kd, L->noise, L->Wt, L->Wx, &ts->Smd0, L->red);
   else TG_CK(cudaMemsetAsync(&ts->Smd0, 0, sizeof(double), s));
   TG_CK(cudaMemcpyAsync(L->Anew, L->A, (size_t)V * sizeof(double2), cudaMemcpyDeviceToDevice, s));
@@ -430,7 +431,7 @@ int enqueue_trajectory(tg_lattice* L, cudaStream_t s, const tg_hmc_params& p, bo
                       1 | (use_noise ? 2 : 0));
     for (int k = 0; k < p.npf; k++) {
       TG_TRY(cg(L->phi + (size_t)k * V, L->chi));
-      dslash64(s, g, km, L->chi, L->Mchi, L->Wt, L->Wx);
+      dslash64(s, g, km, 0, L->chi, L->Mchi, L->Wt, L->Wx);
       int flags = (k == 0 ? 1 : 0) | ((k == p.npf - 1 && use_noise) ? 2 : 0);
       momentum_update(s, g, ep, em, L->Anew, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->mom, eps, gfac, flags);
     }
@@ -440,14 +441,14 @@ int enqueue_trajectory(tg_lattice* L, cudaStream_t s, const tg_hmc_params& p, bo
   TG_CK(cudaMemsetAsync(&ts->Spf1, 0, sizeof(double), s));
   for (int k = 0; k < p.npf; k++) {
     TG_TRY(cg(L->phi + (size_t)k * V, L->chi));
-    redot(s, V, L->phi + (size_t)k * V, L->chi, &ts->Spf1, 1, L->red);
+    redot(s, g, L->phi + (size_t)k * V, L->chi, &ts->Spf1, 1, L->red);
   }
-  norm2(s, V, L->mom, &ts->Smom1, 0, L->red);
-  gauge_action(s, V, L->Anew, kNf / L->P.g, &ts->Sg1, L->red);
+  norm2(s, g, L->mom, &ts->Smom1, 0, L->red);
+  gauge_action(s, g, L->Anew, kNf / L->P.g, &ts->Sg1, L->red);
   if (use_noise) md_action(s, g, kd, L->noise, L->Wt, L->Wx, &ts->Smd1, L->red);
   else TG_CK(cudaMemsetAsync(&ts->Smd1, 0, sizeof(double), s));
   finish_trajectory(s, ts);
-  accept_copy(s, V, ts, L->A, L->Anew);
+  accept_copy(s, g, ts, L->A, L->Anew);
   link_phase(s, g, L->P.bc_t, L->P.bc_x, L->A, L->Wt, L->Wx, L->Wt32, L->Wx32);
   TG_CK(cudaGetLastError());
   return TG_OK;
@@ -529,6 +530,13 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
   L->g.nx = p->nx;
   L->g.V = (int)V;
   L->g.inv_nx = 1.0f / (float)p->nx;
+  {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess || sms <= 0) sms = 1;
+    // 6 resident 256-thread blocks per SM at the kernels' ~40 registers
+    int cap = 6 * sms;
+    L->g.grid = nblocks((int)V) < cap ? nblocks((int)V) : cap;
+  }
   auto bail = [&](int rc) { tg_destroy(L); return rc; };
   if (cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&L->cap2, cudaStreamNonBlocking) != cudaSuccess ||
@@ -640,7 +648,7 @@ int tg_get_gauge(tg_lattice* L, double* A) {
 int tg_apply(tg_lattice* L, const double* in, double* out, int dagger) {
   if (!L || !in || !out) return fail(TG_E_ARG, "null argument");
   TG_TRY(upload(L, L->vin, in, 2 * (size_t)L->V));
-  dslash64(L->stream, L->g, op_k(L, dagger), L->vin, L->vout, L->Wt, L->Wx);
+  dslash64(L->stream, L->g, op_k(L, dagger), dagger, L->vin, L->vout, L->Wt, L->Wx);
   TG_CK(cudaGetLastError());
   return download(L, out, L->vout, 2 * (size_t)L->V);
 }
@@ -648,9 +656,9 @@ int tg_apply(tg_lattice* L, const double* in, double* out, int dagger) {
 int tg_apply_dev(tg_lattice* L, const void* in, void* out, int dagger, int precision) {
   if (!L || !in || !out) return fail(TG_E_ARG, "null argument");
   if (precision == TG_PREC_FP64)
-    dslash64(L->stream, L->g, op_k(L, dagger), (const double2*)in, (double2*)out, L->Wt, L->Wx);
+    dslash64(L->stream, L->g, op_k(L, dagger), dagger, (const double2*)in, (double2*)out, L->Wt, L->Wx);
   else if (precision == TG_PREC_MIXED)
-    dslash32(L->stream, L->g, op_k32(L, dagger), (const float2*)in, (float2*)out, L->Wt32, L->Wx32);
+    dslash32(L->stream, L->g, op_k32(L, dagger), dagger, (const float2*)in, (float2*)out, L->Wt32, L->Wx32);
   else
     return fail(TG_E_ARG, "bad precision");
   TG_CK(cudaGetLastError());
@@ -667,11 +675,11 @@ int tg_time_apply(tg_lattice* L, int n, int dagger, int precision, double* ms_pe
     if (precision == TG_PREC_FP64) {
       const double2* in = (i & 1) ? L->vout : L->vin;
       double2* out = (i & 1) ? L->vin : L->vout;
-      dslash64(L->stream, L->g, op_k(L, dagger), in, out, L->Wt, L->Wx);
+      dslash64(L->stream, L->g, op_k(L, dagger), dagger, in, out, L->Wt, L->Wx);
     } else {
       const float2* in = (i & 1) ? L->wmx.Mps : L->wmx.ps;
       float2* out = (i & 1) ? L->wmx.ps : L->wmx.Mps;
-      dslash32(L->stream, L->g, op_k32(L, dagger), in, out, L->Wt32, L->Wx32);
+      dslash32(L->stream, L->g, op_k32(L, dagger), dagger, in, out, L->Wt32, L->Wx32);
     }
   }
   TG_CK(cudaEventRecord(e1, L->stream));
@@ -705,7 +713,7 @@ int tg_cg_dev(tg_lattice* L, const tg_cg_params* cp, const void* b_dev, void* x_
 
 int tg_gauge_action(tg_lattice* L, double* S) {
   if (!L || !S) return fail(TG_E_ARG, "null argument");
-  gauge_action(L->stream, L->V, L->A, kNf / L->P.g, &L->ts->Sg0, L->red);
+  gauge_action(L->stream, L->g, L->A, kNf / L->P.g, &L->ts->Sg0, L->red);
   TG_CK(cudaGetLastError());
   TG_CK(cudaMemcpyAsync(S, &L->ts->Sg0, sizeof(double), cudaMemcpyDeviceToHost, L->stream));
   TG_CK(cudaStreamSynchronize(L->stream));
@@ -720,7 +728,7 @@ int tg_pseudofermion_action(tg_lattice* L, const tg_cg_params* cp, const double*
   tg_cg_result r{};
   TG_TRY(solve_dev(L, *cp, L->vin, L->vout, &r));
   if (res) *res = r;
-  redot(L->stream, L->V, L->vin, L->vout, &L->ts->Spf1, 0, L->red);
+  redot(L->stream, L->g, L->vin, L->vout, &L->ts->Spf1, 0, L->red);
   TG_CK(cudaGetLastError());
   TG_CK(cudaMemcpyAsync(S, &L->ts->Spf1, sizeof(double), cudaMemcpyDeviceToHost, L->stream));
   TG_CK(cudaStreamSynchronize(L->stream));
@@ -748,7 +756,7 @@ int tg_force(tg_lattice* L, int npf, const double* chi, const double* noise, dou
                 1 | (noise ? 2 : 0));
   for (int k = 0; k < npf; k++) {
     TG_TRY(upload(L, L->chi, chi + 2 * V * k, 2 * V));
-    dslash64(L->stream, L->g, op_k(L, 0), L->chi, L->Mchi, L->Wt, L->Wx);
+    dslash64(L->stream, L->g, op_k(L, 0), 0, L->chi, L->Mchi, L->Wt, L->Wx);
     int flags = (k == 0 ? 1 : 0) | ((k == npf - 1 && noise) ? 2 : 0);
     force_field(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->vout, kNf / L->P.g,
                 flags);
@@ -780,7 +788,7 @@ int tg_momentum_step(tg_lattice* L, const tg_cg_params* cp, double* mom, int npf
     if (r.status > acc.status) acc.status = r.status;
     acc.rr = r.rr;
     acc.rr0 = r.rr0;
-    dslash64(L->stream, L->g, op_k(L, 0), L->chi, L->Mchi, L->Wt, L->Wx);
+    dslash64(L->stream, L->g, op_k(L, 0), 0, L->chi, L->Mchi, L->Wt, L->Wx);
     int flags = (k == 0 ? 1 : 0) | ((k == npf - 1 && noise) ? 2 : 0);
     momentum_update(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->mom, eps, gfac,
                     flags);
@@ -821,7 +829,7 @@ int tg_puregauge_ext(tg_lattice* L, const double* u, int sweeps) {
   for (int sw = 0; sw < sweeps; sw++) {
     // the 2 uniforms of each of the 2V links of one sweep
     TG_TRY(upload(L, L->unif, u + 2 * nl * sw, 2 * nl));
-    puregauge(L->stream, (int)nl, (double*)L->A, L->unif, -kNf / L->P.g);
+    puregauge(L->stream, L->g, (double*)L->A, L->unif, -kNf / L->P.g);
     TG_CK(cudaGetLastError());
   }
   link_phase(L->stream, L->g, L->P.bc_t, L->P.bc_x, L->A, L->Wt, L->Wx, L->Wt32, L->Wx32);

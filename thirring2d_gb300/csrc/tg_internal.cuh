@@ -33,6 +33,16 @@ template <typename R> __device__ __forceinline__ void cmac(C2<R>& acc, C2<R> w, 
   acc.x = fma(w.x, v.x, acc.x); acc.x = fma(-w.y, v.y, acc.x);
   acc.y = fma(w.x, v.y, acc.y); acc.y = fma(w.y, v.x, acc.y);
 }
+// acc -= w * v
+template <typename R> __device__ __forceinline__ void cnmac(C2<R>& acc, C2<R> w, C2<R> v) {
+  acc.x = fma(-w.x, v.x, acc.x); acc.x = fma(w.y, v.y, acc.x);
+  acc.y = fma(-w.x, v.y, acc.y); acc.y = fma(-w.y, v.x, acc.y);
+}
+// acc += conj(w) * v
+template <typename R> __device__ __forceinline__ void cjmac(C2<R>& acc, C2<R> w, C2<R> v) {
+  acc.x = fma(w.x, v.x, acc.x); acc.x = fma(w.y, v.y, acc.x);
+  acc.y = fma(w.x, v.y, acc.y); acc.y = fma(-w.y, v.x, acc.y);
+}
 // acc -= conj(w) * v
 template <typename R> __device__ __forceinline__ void cmsc(C2<R>& acc, C2<R> w, C2<R> v) {
   acc.x = fma(-w.x, v.x, acc.x); acc.x = fma(-w.y, v.y, acc.x);
@@ -51,6 +61,7 @@ template <typename R> __device__ __forceinline__ C2<R> cjmul(C2<R> w, C2<R> v) {
 struct Geo {
   int nt, nx, V;
   float inv_nx;   // for the division-free site -> (t, x) split
+  int grid;       // blocks of a site kernel: min(ceil(V/256), resident blocks of the GPU)
 };
 
 __device__ __forceinline__ void site_tx(const Geo& g, int s, int& t, int& x) {
@@ -71,29 +82,32 @@ __device__ __forceinline__ Nbr neighbours(const Geo& g, int s, int t, int x) {
 }
 
 // Operator constants for M (dag = 0) or the true adjoint M^dagger (dag = 1):
-//   out = m in + cf*Wt in(s+t) + cb*conj(Wt(s-t)) in(s-t) + cx*(Wx in(s+x) - conj(Wx(s-x)) in(s-x))
-// M: cf = e^mu, cb = -e^-mu, cx = +1 (hmc.c:137-180); M^dag: cf = -e^-mu, cb = e^mu, cx = -1.
+//   out = m in + cf*Wt in(s+t) + cb*conj(Wt(s-t)) in(s-t) + sx*(Wx in(s+x) - conj(Wx(s-x)) in(s-x))
+// M: cf = e^mu, cb = -e^-mu, sx = +1 (hmc.c:137-180); M^dag: cf = -e^-mu, cb = e^mu, sx = -1.
+// sx is a template parameter of the kernels; mu0 = (mu == 0) selects the
+// variant without the e^{+-mu} multiplies (18 instead of 22 FMA/MUL per site).
 template <typename R> struct OpK {
-  R m, cf, cb, cx;
+  R m, cf, cb;
+  int mu0;
 };
 
 // ---------------------------------------------------------------------------
 // Block reduction (deterministic: fixed shuffle tree, then fixed smem order)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double warp_sum(double v) {
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
 
-template <int BS> __device__ __forceinline__ double block_sum(double v, double* sh) {
+template <int BS, typename T> __device__ __forceinline__ T block_sum(T v, T* sh) {
   v = warp_sum(v);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) sh[w] = v;
   __syncthreads();
-  double r = 0;
+  T r = 0;
   if (w == 0) {
-    r = (lane < BS / 32) ? sh[lane] : 0.0;
+    r = (lane < BS / 32) ? sh[lane] : T(0);
     r = warp_sum(r);
   }
   __syncthreads();
@@ -101,17 +115,20 @@ template <int BS> __device__ __forceinline__ double block_sum(double v, double* 
 }
 
 // Grid-wide deterministic sum with the "last block finishes" pattern: every
-// block stores its partial, the block that arrives last adds the partials in
-// index order.  Returns true in exactly one block (all its threads), with the
-// total in *total (thread 0 of that block).  `counter` must be 0 on entry
-// and is 0 again on exit.
-template <int BS>
-__device__ __forceinline__ bool grid_sum(double v, double* partials, unsigned* counter, double* total) {
-  __shared__ double sh[BS / 32];
+// block stores its partial (summed in T: float for the FP32 solver, double
+// otherwise), the block that arrives last adds the partials in FP64 in index
+// order.  Returns true in exactly one block (all its threads), with the total
+// in *total (thread 0 of that block).  `counter` must be 0 on entry and is 0
+// again on exit.  Grids are capped near the resident-block count, so the
+// serial part (one atomic per block, one pass over the partials) stays short.
+template <int BS, typename T>
+__device__ __forceinline__ bool grid_sum(T v, double* partials, unsigned* counter, double* total) {
+  __shared__ T sh[BS / 32];
+  __shared__ double shd[BS / 32];
   __shared__ bool is_last;
-  double b = block_sum<BS>(v, sh);
+  T b = block_sum<BS, T>(v, sh);
   if (threadIdx.x == 0) {
-    partials[blockIdx.x] = b;
+    partials[blockIdx.x] = (double)b;
     __threadfence();
     unsigned prev = atomicAdd(counter, 1u);
     is_last = (prev == gridDim.x - 1);
@@ -121,7 +138,7 @@ __device__ __forceinline__ bool grid_sum(double v, double* partials, unsigned* c
   __threadfence();
   double s = 0;
   for (int i = threadIdx.x; i < (int)gridDim.x; i += BS) s += __ldcg(partials + i);
-  s = block_sum<BS>(s, sh);
+  s = block_sum<BS, double>(s, shd);
   if (threadIdx.x == 0) {
     *total = s;
     *counter = 0u;
@@ -130,6 +147,10 @@ __device__ __forceinline__ bool grid_sum(double v, double* partials, unsigned* c
 }
 
 inline int nblocks(int n, int bs = kBlock) { return (n + bs - 1) / bs; }
+inline int grid_of(const Geo& g) { return g.grid; }
+
+// grid-stride loop over the sites of a kernel
+#define TG_SITES(s, n) for (int s = blockIdx.x * kBlock + threadIdx.x; s < (n); s += gridDim.x * kBlock)
 
 // ---------------------------------------------------------------------------
 // Device state of one CG solve.  Lives in device memory; all the scalar

@@ -1,9 +1,10 @@
 // tg_kernels.cu -- sm_103a kernels of the Thirring2D HMC hot path.
 //
-// All kernels are one-thread-per-site over the t-major site index, 256-thread
-// blocks, coalesced double2/float2 loads.  Stencil neighbours along x are in
-// the same or adjacent warps and along t one row (nx sites) away, so each
-// operand is fetched from DRAM once and re-read from L1/L2.  Reductions are
+// Site kernels are grid-stride loops over the t-major site index with
+// 256-thread blocks and a grid capped at the GPU's resident-block count;
+// loads are coalesced double2/float2.  Stencil neighbours along x are in the
+// same or adjacent warps and along t one row (nx sites) away, so each operand
+// comes from DRAM once and is re-read from L1/L2.  Reductions are
 // deterministic (fixed shuffle tree per block, partials summed in index order
 // by the last block), so results do not depend on block scheduling.
 #include <math.h>
@@ -36,80 +37,108 @@ __device__ __forceinline__ void write_links(const Geo& g, int bc_t, int bc_x, in
 
 __global__ void __launch_bounds__(kBlock) k_link_phase(Geo g, int bc_t, int bc_x, const double2* __restrict__ A,
                                                        double2* Wt, double2* Wx, float2* Wt32, float2* Wx32) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s >= g.V) return;
-  write_links(g, bc_t, bc_x, s, A[s], Wt, Wx, Wt32, Wx32);
+  TG_SITES(s, g.V) write_links(g, bc_t, bc_x, s, A[s], Wt, Wx, Wt32, Wx32);
 }
 
-// gauge_step (hmc.c:97-101) applied nadd times: A += c*p with c = 2*eps.
+// gauge_step (hmc.c:97-101) applied nadd times: A += c*p with c = 2*eps,
+// product then sum (two roundings) as the reference's host code computes it.
 __global__ void __launch_bounds__(kBlock) k_gauge_step(Geo g, int bc_t, int bc_x, double2* A,
                                                        const double2* __restrict__ mom, double c, int nadd,
                                                        double2* Wt, double2* Wx, float2* Wt32, float2* Wx32) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s >= g.V) return;
-  double2 a = A[s];
-  double2 p = mom[s];
-  for (int k = 0; k < nadd; k++) {  // product then sum, two roundings, as the host code of hmc.c:99
-    a.x = __dadd_rn(a.x, __dmul_rn(c, p.x));
-    a.y = __dadd_rn(a.y, __dmul_rn(c, p.y));
+  TG_SITES(s, g.V) {
+    double2 a = A[s];
+    double2 p = mom[s];
+    for (int k = 0; k < nadd; k++) {
+      a.x = __dadd_rn(a.x, __dmul_rn(c, p.x));
+      a.y = __dadd_rn(a.y, __dmul_rn(c, p.y));
+    }
+    A[s] = a;
+    write_links(g, bc_t, bc_x, s, a, Wt, Wx, Wt32, Wx32);
   }
-  A[s] = a;
-  write_links(g, bc_t, bc_x, s, a, Wt, Wx, Wt32, Wx32);
 }
 
 void link_phase(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,
                 float2* Wt32, float2* Wx32) {
-  k_link_phase<<<nblocks(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, Wt, Wx, Wt32, Wx32);
+  k_link_phase<<<grid_of(g), kBlock, 0, s>>>(g, bc_t, bc_x, A, Wt, Wx, Wt32, Wx32);
 }
 void gauge_step(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double2* A, const double2* mom, double c,
                 int nadd, double2* Wt, double2* Wx, float2* Wt32, float2* Wx32) {
-  k_gauge_step<<<nblocks(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, mom, c, nadd, Wt, Wx, Wt32, Wx32);
+  k_gauge_step<<<grid_of(g), kBlock, 0, s>>>(g, bc_t, bc_x, A, mom, c, nadd, Wt, Wx, Wt32, Wx32);
 }
 
 // ---------------------------------------------------------------------------
-// The staggered operator at one site (hmc.c:132-183 for M; the true adjoint
-// for M^dagger through the OpK constants).
+// The staggered operator at one site: hmc.c:132-183 for M (DAG = 0) and the
+// true adjoint M^dagger = m - D(-mu) (DAG = 1).  MU0 drops the e^{+-mu}
+// factors (mu = 0): 18 FMA/MUL per site instead of 22.
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, int DAG, bool MU0>
 __device__ __forceinline__ C2<R> dslash_site(const OpK<R>& k, const C2<R>* __restrict__ in,
                                              const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, int s,
                                              const Nbr& n) {
   C2<R> v = in[s];
-  C2<R> ft = cmul<R>(Wt[s], in[n.tp]);
-  C2<R> bt = cjmul<R>(Wt[n.tm], in[n.tm]);
-  C2<R> hx = mk<R>(0, 0);
-  cmac<R>(hx, Wx[s], in[n.xp]);
-  cmsc<R>(hx, Wx[n.xm], in[n.xm]);
-  C2<R> o;
-  o.x = k.m * v.x;
-  o.y = k.m * v.y;
-  o.x = fma(k.cf, ft.x, o.x);
-  o.y = fma(k.cf, ft.y, o.y);
-  o.x = fma(k.cb, bt.x, o.x);
-  o.y = fma(k.cb, bt.y, o.y);
-  o.x = fma(k.cx, hx.x, o.x);
-  o.y = fma(k.cx, hx.y, o.y);
+  C2<R> o = mk<R>(k.m * v.x, k.m * v.y);
+  if (MU0) {
+    if (DAG == 0) {
+      cmac<R>(o, Wt[s], in[n.tp]);
+      cmsc<R>(o, Wt[n.tm], in[n.tm]);
+    } else {
+      cnmac<R>(o, Wt[s], in[n.tp]);
+      cjmac<R>(o, Wt[n.tm], in[n.tm]);
+    }
+  } else {
+    C2<R> ft = cmul<R>(Wt[s], in[n.tp]);
+    C2<R> bt = cjmul<R>(Wt[n.tm], in[n.tm]);
+    o.x = fma(k.cf, ft.x, o.x);
+    o.y = fma(k.cf, ft.y, o.y);
+    o.x = fma(k.cb, bt.x, o.x);
+    o.y = fma(k.cb, bt.y, o.y);
+  }
+  if (DAG == 0) {
+    cmac<R>(o, Wx[s], in[n.xp]);
+    cmsc<R>(o, Wx[n.xm], in[n.xm]);
+  } else {
+    cnmac<R>(o, Wx[s], in[n.xp]);
+    cjmac<R>(o, Wx[n.xm], in[n.xm]);
+  }
   return o;
 }
 
-template <typename R>
+template <typename R, int DAG, bool MU0>
+__device__ __forceinline__ C2<R> dslash_at(const Geo& g, const OpK<R>& k, const C2<R>* __restrict__ in,
+                                           const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, int s) {
+  int t, x;
+  site_tx(g, s, t, x);
+  return dslash_site<R, DAG, MU0>(k, in, Wt, Wx, s, neighbours(g, s, t, x));
+}
+
+template <typename R, int DAG, bool MU0>
 __global__ void __launch_bounds__(kBlock) k_dslash(Geo g, OpK<R> k, const C2<R>* __restrict__ in,
                                                    C2<R>* __restrict__ out, const C2<R>* __restrict__ Wt,
                                                    const C2<R>* __restrict__ Wx) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s >= g.V) return;
-  int t, x;
-  site_tx(g, s, t, x);
-  out[s] = dslash_site<R>(k, in, Wt, Wx, s, neighbours(g, s, t, x));
+  TG_SITES(s, g.V) out[s] = dslash_at<R, DAG, MU0>(g, k, in, Wt, Wx, s);
 }
 
-void dslash64(cudaStream_t s, const Geo& g, const OpK<double>& k, const double2* in, double2* out,
+// launch helper: picks the MU0 instance from the operator constants
+#define TG_OP_DISPATCH(kk, LAUNCH)  \
+  do {                              \
+    if ((kk).mu0) {                 \
+      constexpr bool MU0 = true;    \
+      LAUNCH;                       \
+    } else {                        \
+      constexpr bool MU0 = false;   \
+      LAUNCH;                       \
+    }                               \
+  } while (0)
+
+void dslash64(cudaStream_t s, const Geo& g, const OpK<double>& k, int dag, const double2* in, double2* out,
               const double2* Wt, const double2* Wx) {
-  k_dslash<double><<<nblocks(g.V), kBlock, 0, s>>>(g, k, in, out, Wt, Wx);
+  if (dag) TG_OP_DISPATCH(k, (k_dslash<double, 1, MU0><<<grid_of(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
+  else TG_OP_DISPATCH(k, (k_dslash<double, 0, MU0><<<grid_of(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
 }
-void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, const float2* in, float2* out, const float2* Wt,
-              const float2* Wx) {
-  k_dslash<float><<<nblocks(g.V), kBlock, 0, s>>>(g, k, in, out, Wt, Wx);
+void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, int dag, const float2* in, float2* out,
+              const float2* Wt, const float2* Wx) {
+  if (dag) TG_OP_DISPATCH(k, (k_dslash<float, 1, MU0><<<grid_of(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
+  else TG_OP_DISPATCH(k, (k_dslash<float, 0, MU0><<<grid_of(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
 }
 
 // ---------------------------------------------------------------------------
@@ -119,6 +148,8 @@ void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, const float2* i
 //   K3: p = r + beta p
 // pAp = <p, M^dag M p> is taken as |Mp|^2 (same value, always >= 0).  The
 // scalar recurrences run in the last block of K1/K2, so the host never waits.
+// The FP32 instances (mixed precision) accumulate per-block sums in FP32 and
+// combine the blocks in FP64.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void cg_finish(CgState* st, CgLog* log, int status, Cond c) {
   st->status = status;
@@ -139,19 +170,18 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(Geo g, const double2* __rest
                                                     C2<R>* p, C2<R>* xs, double rel_tol, double abs_tol2,
                                                     int maxiter, int ru_interval, int log_index, CgState* st,
                                                     CgLog* log, Red red, Cond c) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
   double v = 0;
-  if (s < g.V) {
+  TG_SITES(s, g.V) {
     double2 bb = b[s];
     x[s] = make_double2(0.0, 0.0);
     C2<R> rb = mk<R>((R)bb.x, (R)bb.y);
     r[s] = rb;
     p[s] = rb;
     if (xs != nullptr) xs[s] = mk<R>(0, 0);
-    v = bb.x * bb.x + bb.y * bb.y;
+    v += bb.x * bb.x + bb.y * bb.y;
   }
   double tot;
-  if (grid_sum<kBlock>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) {
+  if (grid_sum<kBlock, double>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) {
     double stop = abs_tol2;
     if (rel_tol > 0 && rel_tol * rel_tol * tot > stop) stop = rel_tol * rel_tol * tot;
     st->rr = tot;
@@ -177,22 +207,20 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(Geo g, const double2* __rest
   }
 }
 
-template <typename R>
+template <typename R, bool MU0>
 __global__ void __launch_bounds__(kBlock) k_cg1(Geo g, OpK<R> k, const C2<R>* __restrict__ p, C2<R>* __restrict__ Mp,
                                                 const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx,
                                                 CgState* st, Red red) {
   if (st->done) return;
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  double v = 0;
-  if (s < g.V) {
-    int t, x;
-    site_tx(g, s, t, x);
-    C2<R> o = dslash_site<R>(k, p, Wt, Wx, s, neighbours(g, s, t, x));
+  R v = 0;
+  TG_SITES(s, g.V) {
+    C2<R> o = dslash_at<R, 0, MU0>(g, k, p, Wt, Wx, s);
     Mp[s] = o;
-    v = (double)o.x * (double)o.x + (double)o.y * (double)o.y;
+    v = fma(o.x, o.x, v);
+    v = fma(o.y, o.y, v);
   }
   double tot;
-  if (grid_sum<kBlock>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) {
+  if (grid_sum<kBlock, R>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) {
     st->alpha = st->rr / tot;
     st->need_ru = 0;   // the previous iteration's reliable-update kernels have all run
     st->restart = 0;
@@ -200,6 +228,7 @@ __global__ void __launch_bounds__(kBlock) k_cg1(Geo g, OpK<R> k, const C2<R>* __
 }
 
 // FP64: convergence tested on the recursive residual, as hmc.c:381.
+template <bool MU0>
 __global__ void __launch_bounds__(kBlock) k_cg2_64(Geo g, OpK<double> k, const double2* __restrict__ Mp,
                                                    const double2* __restrict__ p, double2* __restrict__ x,
                                                    double2* __restrict__ r, const double2* __restrict__ Wt,
@@ -207,12 +236,9 @@ __global__ void __launch_bounds__(kBlock) k_cg2_64(Geo g, OpK<double> k, const d
                                                    Red red, Cond c) {
   if (st->done) return;
   const double a = st->alpha;
-  int s = blockIdx.x * kBlock + threadIdx.x;
   double v = 0;
-  if (s < g.V) {
-    int t, xx;
-    site_tx(g, s, t, xx);
-    double2 ap = dslash_site<double>(k, Mp, Wt, Wx, s, neighbours(g, s, t, xx));
+  TG_SITES(s, g.V) {
+    double2 ap = dslash_at<double, 1, MU0>(g, k, Mp, Wt, Wx, s);
     double2 xv = x[s], pv = p[s], rv = r[s];
     xv.x += a * pv.x;
     xv.y += a * pv.y;
@@ -220,10 +246,11 @@ __global__ void __launch_bounds__(kBlock) k_cg2_64(Geo g, OpK<double> k, const d
     rv.y -= a * ap.y;
     x[s] = xv;
     r[s] = rv;
-    v = rv.x * rv.x + rv.y * rv.y;
+    v = fma(rv.x, rv.x, v);
+    v = fma(rv.y, rv.y, v);
   }
   double rn;
-  if (grid_sum<kBlock>(v, red.partials, red.counter, &rn) && threadIdx.x == 0) {
+  if (grid_sum<kBlock, double>(v, red.partials, red.counter, &rn) && threadIdx.x == 0) {
     st->iter += 1;
     double rr_old = st->rr;
     st->rr = rn;
@@ -240,44 +267,43 @@ __global__ void __launch_bounds__(kBlock) k_cg3(int n, const C2<R>* __restrict__
                                                 const CgState* st) {
   if (st->done) return;
   const R b = (R)st->beta;
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s >= n) return;
-  C2<R> rv = r[s], pv = p[s];
-  p[s] = mk<R>(rv.x + b * pv.x, rv.y + b * pv.y);
+  TG_SITES(s, n) {
+    C2<R> rv = r[s], pv = p[s];
+    p[s] = mk<R>(fma(b, pv.x, rv.x), fma(b, pv.y, rv.y));
+  }
 }
 
 void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
                CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int log_index, Cond c) {
-  k_cg_init<double><<<nblocks(g.V), kBlock, 0, s>>>(g, b, x, w.r, w.p, nullptr, rel_tol, abs_tol2, maxiter, 0,
-                                                    log_index, st, log, red, c);
+  k_cg_init<double><<<grid_of(g), kBlock, 0, s>>>(g, b, x, w.r, w.p, nullptr, rel_tol, abs_tol2, maxiter, 0,
+                                                  log_index, st, log, red, c);
 }
 
 void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
                double2* x, const CgBufs64& w, CgState* st, CgLog* log, const Red& red, Cond c) {
-  int nb = nblocks(g.V);
-  k_cg1<double><<<nb, kBlock, 0, s>>>(g, km, w.p, w.Mp, L.Wt, L.Wx, st, red);
-  k_cg2_64<<<nb, kBlock, 0, s>>>(g, kd, w.Mp, w.p, x, w.r, L.Wt, L.Wx, st, log, red, c);
+  const int nb = grid_of(g);
+  TG_OP_DISPATCH(km, (k_cg1<double, MU0><<<nb, kBlock, 0, s>>>(g, km, w.p, w.Mp, L.Wt, L.Wx, st, red)));
+  TG_OP_DISPATCH(kd, (k_cg2_64<MU0><<<nb, kBlock, 0, s>>>(g, kd, w.Mp, w.p, x, w.r, L.Wt, L.Wx, st, log, red, c)));
   k_cg3<double><<<nb, kBlock, 0, s>>>(g.V, w.r, w.p, st);
 }
 
 // ---------------------------------------------------------------------------
 // Mixed precision: FP32 vectors and links, FP64 scalar recurrences.  x
-// accumulates in FP64 at each reliable update (every ru_interval iterations,
-// when the FP32 residual reaches the target, or at the iteration cap), which
-// recomputes r = b - M^dag M x in FP64 and restarts the FP32 residual from it.
+// accumulates in FP64 at each reliable update, which recomputes
+// r = b - M^dag M x in FP64 and restarts the FP32 residual from it.  Updates
+// happen every ru_interval iterations, once |r|^2 has fallen by kRuDrop since
+// the last one, when the FP32 residual reaches the target, and at the cap.
 // ---------------------------------------------------------------------------
+template <bool MU0>
 __global__ void __launch_bounds__(kBlock) k_cgmx2(Geo g, OpK<float> k, const float2* __restrict__ Mp,
                                                   const float2* __restrict__ p, float2* __restrict__ xs,
                                                   float2* __restrict__ r, const float2* __restrict__ Wt,
                                                   const float2* __restrict__ Wx, CgState* st, Red red, Cond c) {
   if (st->done) return;
   const float a = (float)st->alpha;
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  double v = 0;
-  if (s < g.V) {
-    int t, xx;
-    site_tx(g, s, t, xx);
-    float2 ap = dslash_site<float>(k, Mp, Wt, Wx, s, neighbours(g, s, t, xx));
+  float v = 0;
+  TG_SITES(s, g.V) {
+    float2 ap = dslash_at<float, 1, MU0>(g, k, Mp, Wt, Wx, s);
     float2 xv = xs[s], pv = p[s], rv = r[s];
     xv.x = fmaf(a, pv.x, xv.x);
     xv.y = fmaf(a, pv.y, xv.y);
@@ -285,10 +311,11 @@ __global__ void __launch_bounds__(kBlock) k_cgmx2(Geo g, OpK<float> k, const flo
     rv.y = fmaf(-a, ap.y, rv.y);
     xs[s] = xv;
     r[s] = rv;
-    v = (double)rv.x * rv.x + (double)rv.y * rv.y;
+    v = fmaf(rv.x, rv.x, v);
+    v = fmaf(rv.y, rv.y, v);
   }
   double rn;
-  if (grid_sum<kBlock>(v, red.partials, red.counter, &rn) && threadIdx.x == 0) {
+  if (grid_sum<kBlock, float>(v, red.partials, red.counter, &rn) && threadIdx.x == 0) {
     st->iter += 1;
     st->since_ru += 1;
     double rr_old = st->rr;
@@ -304,47 +331,43 @@ __global__ void __launch_bounds__(kBlock) k_cgmx2(Geo g, OpK<float> k, const flo
 // reliable update 1: x += xs, xs = 0
 __global__ void __launch_bounds__(kBlock) k_ru1(int n, double2* x, float2* xs, const CgState* st) {
   if (!st->need_ru || st->done) return;
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s >= n) return;
-  float2 d = xs[s];
-  double2 v = x[s];
-  v.x += (double)d.x;
-  v.y += (double)d.y;
-  x[s] = v;
-  xs[s] = make_float2(0.f, 0.f);
+  TG_SITES(s, n) {
+    float2 d = xs[s];
+    double2 v = x[s];
+    v.x += (double)d.x;
+    v.y += (double)d.y;
+    x[s] = v;
+    xs[s] = make_float2(0.f, 0.f);
+  }
 }
 
 // reliable update 2: tmp = M x (FP64)
+template <bool MU0>
 __global__ void __launch_bounds__(kBlock) k_ru2(Geo g, OpK<double> k, const double2* __restrict__ x,
                                                 double2* __restrict__ tmp, const double2* __restrict__ Wt,
                                                 const double2* __restrict__ Wx, const CgState* st) {
   if (!st->need_ru || st->done) return;
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s >= g.V) return;
-  int t, xx;
-  site_tx(g, s, t, xx);
-  tmp[s] = dslash_site<double>(k, x, Wt, Wx, s, neighbours(g, s, t, xx));
+  TG_SITES(s, g.V) tmp[s] = dslash_at<double, 0, MU0>(g, k, x, Wt, Wx, s);
 }
 
 // reliable update 3: r = b - M^dag tmp (FP64), rs = (float) r, decide
+template <bool MU0>
 __global__ void __launch_bounds__(kBlock) k_ru3(Geo g, OpK<double> k, const double2* __restrict__ b,
                                                 const double2* __restrict__ tmp, float2* __restrict__ rs,
                                                 const double2* __restrict__ Wt, const double2* __restrict__ Wx,
                                                 CgState* st, CgLog* log, Red red, Cond c) {
   if (!st->need_ru || st->done) return;
-  int s = blockIdx.x * kBlock + threadIdx.x;
   double v = 0;
-  if (s < g.V) {
-    int t, xx;
-    site_tx(g, s, t, xx);
-    double2 ap = dslash_site<double>(k, tmp, Wt, Wx, s, neighbours(g, s, t, xx));
+  TG_SITES(s, g.V) {
+    double2 ap = dslash_at<double, 1, MU0>(g, k, tmp, Wt, Wx, s);
     double2 bb = b[s];
     double2 rv = make_double2(bb.x - ap.x, bb.y - ap.y);
     rs[s] = make_float2((float)rv.x, (float)rv.y);
-    v = rv.x * rv.x + rv.y * rv.y;
+    v = fma(rv.x, rv.x, v);
+    v = fma(rv.y, rv.y, v);
   }
   double rt;
-  if (grid_sum<kBlock>(v, red.partials, red.counter, &rt) && threadIdx.x == 0) {
+  if (grid_sum<kBlock, double>(v, red.partials, red.counter, &rt) && threadIdx.x == 0) {
     st->restart = rt > kRuRestart * st->rr;  // recursive residual was far too optimistic
     st->rr_true = rt;
     st->rr = rt;
@@ -361,32 +384,32 @@ __global__ void __launch_bounds__(kBlock) k_ru3(Geo g, OpK<double> k, const doub
 __global__ void __launch_bounds__(kBlock) k_ru4(int n, const float2* __restrict__ rs, float2* __restrict__ ps,
                                                 const CgState* st) {
   if (!st->need_ru || !st->restart || st->done) return;
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s < n) ps[s] = rs[s];
+  TG_SITES(s, n) ps[s] = rs[s];
 }
 
 void cgmx_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufsMixed& w, CgState* st,
                CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int ru_interval,
                int log_index, Cond c) {
-  k_cg_init<float><<<nblocks(g.V), kBlock, 0, s>>>(g, b, x, w.rs, w.ps, w.xs, rel_tol, abs_tol2, maxiter,
-                                                   ru_interval, log_index, st, log, red, c);
+  k_cg_init<float><<<grid_of(g), kBlock, 0, s>>>(g, b, x, w.rs, w.ps, w.xs, rel_tol, abs_tol2, maxiter,
+                                                 ru_interval, log_index, st, log, red, c);
 }
 
 void cgmx_iter(cudaStream_t s, const Geo& g, const OpK<float>& km, const OpK<float>& kd, const Links& L,
                const CgBufsMixed& w, CgState* st, const Red& red, Cond c) {
-  int nb = nblocks(g.V);
-  k_cg1<float><<<nb, kBlock, 0, s>>>(g, km, w.ps, w.Mps, L.Wt32, L.Wx32, st, red);
-  k_cgmx2<<<nb, kBlock, 0, s>>>(g, kd, w.Mps, w.ps, w.xs, w.rs, L.Wt32, L.Wx32, st, red, c);
+  const int nb = grid_of(g);
+  TG_OP_DISPATCH(km, (k_cg1<float, MU0><<<nb, kBlock, 0, s>>>(g, km, w.ps, w.Mps, L.Wt32, L.Wx32, st, red)));
+  TG_OP_DISPATCH(kd,
+                 (k_cgmx2<MU0><<<nb, kBlock, 0, s>>>(g, kd, w.Mps, w.ps, w.xs, w.rs, L.Wt32, L.Wx32, st, red, c)));
   k_cg3<float><<<nb, kBlock, 0, s>>>(g.V, w.rs, w.ps, st);
 }
 
 void cgmx_reliable(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
                    const double2* b, double2* x, const CgBufsMixed& w, CgState* st, CgLog* log, const Red& red,
                    Cond c) {
-  int nb = nblocks(g.V);
+  const int nb = grid_of(g);
   k_ru1<<<nb, kBlock, 0, s>>>(g.V, x, w.xs, st);
-  k_ru2<<<nb, kBlock, 0, s>>>(g, km, x, w.tmp64, L.Wt, L.Wx, st);
-  k_ru3<<<nb, kBlock, 0, s>>>(g, kd, b, w.tmp64, w.rs, L.Wt, L.Wx, st, log, red, c);
+  TG_OP_DISPATCH(km, (k_ru2<MU0><<<nb, kBlock, 0, s>>>(g, km, x, w.tmp64, L.Wt, L.Wx, st)));
+  TG_OP_DISPATCH(kd, (k_ru3<MU0><<<nb, kBlock, 0, s>>>(g, kd, b, w.tmp64, w.rs, L.Wt, L.Wx, st, log, red, c)));
   k_ru4<<<nb, kBlock, 0, s>>>(g.V, w.rs, w.ps, st);
 }
 
@@ -395,68 +418,66 @@ void cgmx_reliable(cudaStream_t s, const Geo& g, const OpK<double>& km, const Op
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_norm2(int n, const double2* __restrict__ v, double* dst, int acc,
                                                   Red red) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
   double a = 0;
-  if (s < n) {
+  TG_SITES(s, n) {
     double2 u = v[s];
-    a = u.x * u.x + u.y * u.y;
+    a += u.x * u.x + u.y * u.y;
   }
   double tot;
-  if (grid_sum<kBlock>(a, red.partials, red.counter, &tot) && threadIdx.x == 0) *dst = acc ? *dst + tot : tot;
+  if (grid_sum<kBlock, double>(a, red.partials, red.counter, &tot) && threadIdx.x == 0)
+    *dst = acc ? *dst + tot : tot;
 }
 
 __global__ void __launch_bounds__(kBlock) k_redot(int n, const double2* __restrict__ u, const double2* __restrict__ v,
                                                   double* dst, int acc, Red red) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
   double a = 0;
-  if (s < n) {
+  TG_SITES(s, n) {
     double2 x = u[s], y = v[s];
-    a = x.x * y.x + x.y * y.y;
+    a += x.x * y.x + x.y * y.y;
   }
   double tot;
-  if (grid_sum<kBlock>(a, red.partials, red.counter, &tot) && threadIdx.x == 0) *dst = acc ? *dst + tot : tot;
+  if (grid_sum<kBlock, double>(a, red.partials, red.counter, &tot) && threadIdx.x == 0)
+    *dst = acc ? *dst + tot : tot;
 }
 
 __global__ void __launch_bounds__(kBlock) k_gauge_action(int n, const double2* __restrict__ A, double fac,
                                                          double* dst, Red red) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
   double a = 0;
-  if (s < n) {
+  TG_SITES(s, n) {
     double2 v = A[s];
-    a = (1. - cos(v.x)) + (1. - cos(v.y));
+    a += (1. - cos(v.x)) + (1. - cos(v.y));
   }
   double tot;
-  if (grid_sum<kBlock>(a, red.partials, red.counter, &tot) && threadIdx.x == 0) *dst = fac * tot;
+  if (grid_sum<kBlock, double>(a, red.partials, red.counter, &tot) && threadIdx.x == 0) *dst = fac * tot;
 }
 
+template <bool MU0>
 __global__ void __launch_bounds__(kBlock) k_md_action(Geo g, OpK<double> k, const double2* __restrict__ nz,
                                                       const double2* __restrict__ Wt, const double2* __restrict__ Wx,
                                                       double* dst, Red red) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
   double a = 0;
-  if (s < g.V) {
-    int t, x;
-    site_tx(g, s, t, x);
-    double2 o = dslash_site<double>(k, nz, Wt, Wx, s, neighbours(g, s, t, x));
+  TG_SITES(s, g.V) {
+    double2 o = dslash_at<double, 1, MU0>(g, k, nz, Wt, Wx, s);
     double2 v = nz[s];
-    a = v.x * o.x + v.y * o.y;
+    a += v.x * o.x + v.y * o.y;
   }
   double tot;
-  if (grid_sum<kBlock>(a, red.partials, red.counter, &tot) && threadIdx.x == 0) *dst = tot;
+  if (grid_sum<kBlock, double>(a, red.partials, red.counter, &tot) && threadIdx.x == 0) *dst = tot;
 }
 
-void norm2(cudaStream_t s, int n, const double2* v, double* dst, int accumulate, const Red& red) {
-  k_norm2<<<nblocks(n), kBlock, 0, s>>>(n, v, dst, accumulate, red);
+void norm2(cudaStream_t s, const Geo& g, const double2* v, double* dst, int accumulate, const Red& red) {
+  k_norm2<<<grid_of(g), kBlock, 0, s>>>(g.V, v, dst, accumulate, red);
 }
-void redot(cudaStream_t s, int n, const double2* u, const double2* v, double* dst, int accumulate, const Red& red) {
-  k_redot<<<nblocks(n), kBlock, 0, s>>>(n, u, v, dst, accumulate, red);
+void redot(cudaStream_t s, const Geo& g, const double2* u, const double2* v, double* dst, int accumulate,
+           const Red& red) {
+  k_redot<<<grid_of(g), kBlock, 0, s>>>(g.V, u, v, dst, accumulate, red);
 }
-void gauge_action(cudaStream_t s, int n, const double2* A, double fac, double* dst, const Red& red) {
-  k_gauge_action<<<nblocks(n), kBlock, 0, s>>>(n, A, fac, dst, red);
+void gauge_action(cudaStream_t s, const Geo& g, const double2* A, double fac, double* dst, const Red& red) {
+  k_gauge_action<<<grid_of(g), kBlock, 0, s>>>(g.V, A, fac, dst, red);
 }
 void md_action(cudaStream_t s, const Geo& g, const OpK<double>& kd, const double2* nz, const double2* Wt,
                const double2* Wx, double* dst, const Red& red) {
-  k_md_action<<<nblocks(g.V), kBlock, 0, s>>>(g, kd, nz, Wt, Wx, dst, red);
+  TG_OP_DISPATCH(kd, (k_md_action<MU0><<<grid_of(g), kBlock, 0, s>>>(g, kd, nz, Wt, Wx, dst, red)));
 }
 
 // ---------------------------------------------------------------------------
@@ -511,23 +532,23 @@ __global__ void __launch_bounds__(kBlock) k_momentum_update(Geo g, double ep, do
                                                             const double2* __restrict__ Mchi,
                                                             const double2* __restrict__ noise, double2* mom,
                                                             double eps, double gfac, int flags) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s >= g.V) return;
-  ForcePieces f = force_site(g, ep, em, A, Wt, Wx, chi, Mchi, (flags & 2) ? noise : nullptr, s);
-  double2 p = mom[s];
-  if (flags & 1) {
-    p.x -= gfac * f.g.x;
-    p.y -= gfac * f.g.y;
+  TG_SITES(s, g.V) {
+    ForcePieces f = force_site(g, ep, em, A, Wt, Wx, chi, Mchi, (flags & 2) ? noise : nullptr, s);
+    double2 p = mom[s];
+    if (flags & 1) {
+      p.x -= gfac * f.g.x;
+      p.y -= gfac * f.g.y;
+    }
+    if (chi != nullptr) {
+      p.x -= eps * f.pf.x;
+      p.y -= eps * f.pf.y;
+    }
+    if (flags & 2) {
+      p.x -= eps * f.md.x;
+      p.y -= eps * f.md.y;
+    }
+    mom[s] = p;
   }
-  if (chi != nullptr) {
-    p.x -= eps * f.pf.x;
-    p.y -= eps * f.pf.y;
-  }
-  if (flags & 2) {
-    p.x -= eps * f.md.x;
-    p.y -= eps * f.md.y;
-  }
-  mom[s] = p;
 }
 
 __global__ void __launch_bounds__(kBlock) k_force_field(Geo g, double ep, double em, const double2* __restrict__ A,
@@ -536,28 +557,28 @@ __global__ void __launch_bounds__(kBlock) k_force_field(Geo g, double ep, double
                                                         const double2* __restrict__ Mchi,
                                                         const double2* __restrict__ noise, double2* F, double gfac,
                                                         int flags) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s >= g.V) return;
-  ForcePieces f = force_site(g, ep, em, A, Wt, Wx, chi, Mchi, (flags & 2) ? noise : nullptr, s);
-  double2 o = F[s];
-  if (flags & 1) {
-    o.x += gfac * f.g.x;
-    o.y += gfac * f.g.y;
+  TG_SITES(s, g.V) {
+    ForcePieces f = force_site(g, ep, em, A, Wt, Wx, chi, Mchi, (flags & 2) ? noise : nullptr, s);
+    double2 o = F[s];
+    if (flags & 1) {
+      o.x += gfac * f.g.x;
+      o.y += gfac * f.g.y;
+    }
+    o.x += f.pf.x + f.md.x;
+    o.y += f.pf.y + f.md.y;
+    F[s] = o;
   }
-  o.x += f.pf.x + f.md.x;
-  o.y += f.pf.y + f.md.y;
-  F[s] = o;
 }
 
 void momentum_update(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
                      const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise,
                      double2* mom, double eps, double gfac, int flags) {
-  k_momentum_update<<<nblocks(g.V), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, mom, eps, gfac, flags);
+  k_momentum_update<<<grid_of(g), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, mom, eps, gfac, flags);
 }
 void force_field(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
                  const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise, double2* F,
                  double gfac, int flags) {
-  k_force_field<<<nblocks(g.V), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, F, gfac, flags);
+  k_force_field<<<grid_of(g), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, F, gfac, flags);
 }
 
 // ---------------------------------------------------------------------------
@@ -585,16 +606,16 @@ __device__ __forceinline__ double u53(unsigned hi, unsigned lo) {
 
 __global__ void __launch_bounds__(kBlock) k_philox_gauss(int n, unsigned long long seed, const TrajStats* ts,
                                                          unsigned stream_id, double2* out) {
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s >= n) return;
-  unsigned long long tr = ts->traj;
-  uint4 r = philox4x32(make_uint4((unsigned)s, stream_id, (unsigned)tr, (unsigned)(tr >> 32)),
-                       make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
-  double u1 = u53(r.x, r.y), u2 = u53(r.z, r.w);
-  double rad = sqrt(-2.0 * log(u1));
-  double sn, cs;
-  sincospi(2.0 * u2, &sn, &cs);
-  out[s] = make_double2(rad * cs, rad * sn);
+  const unsigned long long tr = ts->traj;
+  TG_SITES(s, n) {
+    uint4 r = philox4x32(make_uint4((unsigned)s, stream_id, (unsigned)tr, (unsigned)(tr >> 32)),
+                         make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+    double u1 = u53(r.x, r.y), u2 = u53(r.z, r.w);
+    double rad = sqrt(-2.0 * log(u1));
+    double sn, cs;
+    sincospi(2.0 * u2, &sn, &cs);
+    out[s] = make_double2(rad * cs, rad * sn);
+  }
 }
 
 __global__ void k_philox_uniform(unsigned long long seed, TrajStats* ts, unsigned stream_id) {
@@ -604,9 +625,9 @@ __global__ void k_philox_uniform(unsigned long long seed, TrajStats* ts, unsigne
   ts->u = u53(r.x, r.y);
 }
 
-void philox_gauss(cudaStream_t s, int n, unsigned long long seed, const TrajStats* ts, unsigned stream_id,
+void philox_gauss(cudaStream_t s, const Geo& g, unsigned long long seed, const TrajStats* ts, unsigned stream_id,
                   double2* out) {
-  k_philox_gauss<<<nblocks(n), kBlock, 0, s>>>(n, seed, ts, stream_id, out);
+  k_philox_gauss<<<grid_of(g), kBlock, 0, s>>>(g.V, seed, ts, stream_id, out);
 }
 void philox_uniform(cudaStream_t s, unsigned long long seed, TrajStats* ts, unsigned stream_id) {
   k_philox_uniform<<<1, 1, 0, s>>>(seed, ts, stream_id);
@@ -618,17 +639,17 @@ void philox_uniform(cudaStream_t s, unsigned long long seed, TrajStats* ts, unsi
 // reference's order (proposal, then acceptance).  c = -Nf/g.  The proposal is
 // computed without FMA contraction so it is bit-identical to the host's.
 __global__ void __launch_bounds__(kBlock) k_puregauge(int n, double* A, const double* __restrict__ u, double c) {
-  int k = blockIdx.x * kBlock + threadIdx.x;
-  if (k >= n) return;
-  double a = A[k];
-  double s1 = c * cos(a);
-  double prop = __dsub_rn(__dmul_rn(2 * M_PI, u[2 * k]), M_PI);
-  double s2 = c * cos(prop);
-  if (u[2 * k + 1] < exp(-s2 + s1)) A[k] = prop;
+  TG_SITES(k, n) {
+    double a = A[k];
+    double s1 = c * cos(a);
+    double prop = __dsub_rn(__dmul_rn(2 * M_PI, u[2 * k]), M_PI);
+    double s2 = c * cos(prop);
+    if (u[2 * k + 1] < exp(-s2 + s1)) A[k] = prop;
+  }
 }
 
-void puregauge(cudaStream_t s, int nlinks, double* A, const double* u, double c) {
-  k_puregauge<<<nblocks(nlinks), kBlock, 0, s>>>(nlinks, A, u, c);
+void puregauge(cudaStream_t s, const Geo& g, double* A, const double* u, double c) {
+  k_puregauge<<<grid_of(g), kBlock, 0, s>>>(2 * g.V, A, u, c);
 }
 
 // dH in the order of hmc.c:729-732, accept if exp(-dH) > u (hmc.c:738)
@@ -642,13 +663,12 @@ __global__ void k_finish(TrajStats* ts) {
 __global__ void __launch_bounds__(kBlock) k_accept_copy(int n, const TrajStats* ts, double2* A,
                                                         const double2* __restrict__ Anew) {
   if (!ts->accepted) return;
-  int s = blockIdx.x * kBlock + threadIdx.x;
-  if (s < n) A[s] = Anew[s];
+  TG_SITES(s, n) A[s] = Anew[s];
 }
 
 void finish_trajectory(cudaStream_t s, TrajStats* ts) { k_finish<<<1, 1, 0, s>>>(ts); }
-void accept_copy(cudaStream_t s, int n, const TrajStats* ts, double2* A, const double2* Anew) {
-  k_accept_copy<<<nblocks(n), kBlock, 0, s>>>(n, ts, A, Anew);
+void accept_copy(cudaStream_t s, const Geo& g, const TrajStats* ts, double2* A, const double2* Anew) {
+  k_accept_copy<<<grid_of(g), kBlock, 0, s>>>(g.V, ts, A, Anew);
 }
 
 }  // namespace tg

@@ -38,10 +38,11 @@ void link_phase(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2*
 // A += c*mom, nadd times in sequence, then link coefficients
 void gauge_step(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double2* A, const double2* mom, double c,
                 int nadd, double2* Wt, double2* Wx, float2* Wt32, float2* Wx32);
-void dslash64(cudaStream_t s, const Geo& g, const OpK<double>& k, const double2* in, double2* out,
+// out = M in (dag = 0) or M^dag in (dag = 1); k must be the constants of that operator
+void dslash64(cudaStream_t s, const Geo& g, const OpK<double>& k, int dag, const double2* in, double2* out,
               const double2* Wt, const double2* Wx);
-void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, const float2* in, float2* out, const float2* Wt,
-              const float2* Wx);
+void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, int dag, const float2* in, float2* out,
+              const float2* Wt, const float2* Wx);
 
 // CG on M^dag M (FP64).  km = M constants, kd = M^dag constants.
 void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
@@ -59,9 +60,10 @@ void cgmx_reliable(cudaStream_t s, const Geo& g, const OpK<double>& km, const Op
                    Cond c);
 
 // reductions into a device double (accumulate: *dst += sum, else *dst = sum)
-void norm2(cudaStream_t s, int n, const double2* v, double* dst, int accumulate, const Red& red);
-void redot(cudaStream_t s, int n, const double2* u, const double2* v, double* dst, int accumulate, const Red& red);
-void gauge_action(cudaStream_t s, int n, const double2* A, double fac, double* dst, const Red& red);
+void norm2(cudaStream_t s, const Geo& g, const double2* v, double* dst, int accumulate, const Red& red);
+void redot(cudaStream_t s, const Geo& g, const double2* u, const double2* v, double* dst, int accumulate,
+           const Red& red);
+void gauge_action(cudaStream_t s, const Geo& g, const double2* A, double fac, double* dst, const Red& red);
 void md_action(cudaStream_t s, const Geo& g, const OpK<double>& kd, const double2* nz, const double2* Wt,
                const double2* Wx, double* dst, const Red& red);
 
@@ -75,13 +77,13 @@ void force_field(cudaStream_t s, const Geo& g, double ep, double em, const doubl
                  double gfac, int flags);
 
 // Philox Gaussian fields: out[n] complex pairs for (seed, stats->traj, stream_id)
-void philox_gauss(cudaStream_t s, int n, unsigned long long seed, const TrajStats* ts, unsigned stream_id,
+void philox_gauss(cudaStream_t s, const Geo& g, unsigned long long seed, const TrajStats* ts, unsigned stream_id,
                   double2* out);
 void philox_uniform(cudaStream_t s, unsigned long long seed, TrajStats* ts, unsigned stream_id);
 
 void finish_trajectory(cudaStream_t s, TrajStats* ts);
-void accept_copy(cudaStream_t s, int n, const TrajStats* ts, double2* A, const double2* Anew);
-// one pure-gauge Metropolis sweep over nlinks = 2V links; u[2*nlinks]; c = -Nf/g
-void puregauge(cudaStream_t s, int nlinks, double* A, const double* u, double c);
+void accept_copy(cudaStream_t s, const Geo& g, const TrajStats* ts, double2* A, const double2* Anew);
+// one pure-gauge Metropolis sweep over the 2V links; u[4V]; c = -Nf/g
+void puregauge(cudaStream_t s, const Geo& g, double* A, const double* u, double c);
 
 }  // namespace tg
