@@ -313,3 +313,23 @@ def test_errors_are_reported(tg):
         L.update_gauge(tg.hmc_params(npf=9))
     with pytest.raises(tg.native.TGError):
         L.update_gauge(tg.hmc_params(nsteps=0))
+
+
+@pytest.mark.parametrize("nt,nx,mu", [(32, 32, 0.0), (64, 96, 0.3), (8, 64, 0.1)])
+def test_column_march_equals_site_path(tg, monkeypatch, nt, nx, mu):
+    """The warp column march (nx % 32 == 0) computes the same operator values,
+    bit for bit, as the one-site-per-thread path, and the same CG solution."""
+    rng = np.random.default_rng(nt + nx)
+    A = rng.normal(0, 0.6, (nt, nx, 2))
+    psi = cplx(rng, (nt, nx))
+    out = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("TG_MARCH", flag)
+        L = tg.Lattice(nt, nx, 0.2, 0.5, mu, -1, 1)
+        L.set_gauge(A)
+        x, res = L.fmdm_invert_cg(psi, tg.cg_params(rel_tol=1e-12, abs_tol2=0))
+        xm, resm = L.fmdm_invert_cg(psi, tg.cg_params(rel_tol=1e-12, abs_tol2=0, precision=1))
+        out.append((L.fm_mul(psi), L.fm_conjugate_mul(psi), x, xm, res.iterations))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert rel(out[0][2], out[1][2]) < 1e-10 and rel(out[0][3], out[1][3]) < 1e-9
+    assert abs(out[0][4] - out[1][4]) <= 2

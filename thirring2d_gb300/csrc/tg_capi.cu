@@ -533,9 +533,14 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
   {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess || sms <= 0) sms = 1;
-    // 6 resident 256-thread blocks per SM at the kernels' ~40 registers
-    int cap = 6 * sms;
+    // 8 resident 256-thread blocks per SM at <= 32 registers per thread
+    int cap = 8 * sms;
     L->g.grid = nblocks((int)V) < cap ? nblocks((int)V) : cap;
+    const char* e = getenv("TG_MARCH");
+    L->g.march = (p->nx % 32 == 0) && (p->nt % kMarchT == 0) && !(e && e[0] == '0');
+    int items = L->g.march ? (p->nx / 32) * (p->nt / kMarchT) : 0;
+    int mg = (items + kBlock / 32 - 1) / (kBlock / 32);
+    L->g.mgrid = L->g.march ? (mg < cap ? mg : cap) : L->g.grid;
   }
   auto bail = [&](int rc) { tg_destroy(L); return rc; };
   if (cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking) != cudaSuccess ||

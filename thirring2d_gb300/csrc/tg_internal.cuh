@@ -61,8 +61,17 @@ template <typename R> __device__ __forceinline__ C2<R> cjmul(C2<R> w, C2<R> v) {
 struct Geo {
   int nt, nx, V;
   float inv_nx;   // for the division-free site -> (t, x) split
-  int grid;       // blocks of a site kernel: min(ceil(V/256), resident blocks of the GPU)
+  int grid;       // blocks of a reducing site kernel: min(ceil(V/256), resident blocks of the GPU)
+  int march;      // 1: stencil kernels use the warp column march (nx % 32 == 0, nt % kMarchT == 0)
+  int mgrid;      // blocks of a column-march kernel
 };
+
+// Column march: a warp owns 32 consecutive x of one row block and walks
+// kMarchT rows in t, keeping psi(t-1), psi(t) and Wt(t-1) in registers; the
+// x neighbours come from warp shuffles (lanes 0 and 31 load the ones across
+// the warp's edge).  Per site that leaves 3 coalesced loads (psi(t+1), Wt,
+// Wx) instead of 9.
+constexpr int kMarchT = 4;
 
 __device__ __forceinline__ void site_tx(const Geo& g, int s, int& t, int& x) {
   // V < 2^24 keeps float(s) exact; the fix-up absorbs the rounding of s/nx.
@@ -148,6 +157,7 @@ __device__ __forceinline__ bool grid_sum(T v, double* partials, unsigned* counte
 
 inline int nblocks(int n, int bs = kBlock) { return (n + bs - 1) / bs; }
 inline int grid_of(const Geo& g) { return g.grid; }
+inline int stream_grid(int n) { return nblocks(n); }  // streaming kernels without reductions
 
 // grid-stride loop over the sites of a kernel
 #define TG_SITES(s, n) for (int s = blockIdx.x * kBlock + threadIdx.x; s < (n); s += gridDim.x * kBlock)

@@ -1,12 +1,14 @@
 // tg_kernels.cu -- sm_103a kernels of the Thirring2D HMC hot path.
 //
-// Site kernels are grid-stride loops over the t-major site index with
-// 256-thread blocks and a grid capped at the GPU's resident-block count;
-// loads are coalesced double2/float2.  Stencil neighbours along x are in the
-// same or adjacent warps and along t one row (nx sites) away, so each operand
-// comes from DRAM once and is re-read from L1/L2.  Reductions are
-// deterministic (fixed shuffle tree per block, partials summed in index order
-// by the last block), so results do not depend on block scheduling.
+// Stencil kernels (operator applies and the CG kernels built on them) use the
+// warp column march of stencil_all(): a warp walks kMarchT rows of 32
+// consecutive x, reusing psi(t-1), psi(t), Wt(t-1) from registers and taking
+// x neighbours from warp shuffles, with the CG vector updates and norms fused
+// into the per-site epilogue.  Lattices whose nx is not a multiple of 32 (or
+// nt of kMarchT) use one site per thread.  Streaming kernels are one site per
+// thread over the full grid.  Reductions are deterministic (fixed shuffle
+// tree per block, partials summed in index order by the last block), so
+// results do not depend on block scheduling.
 #include <math.h>
 
 #include "tg_launch.h"
@@ -59,11 +61,11 @@ __global__ void __launch_bounds__(kBlock) k_gauge_step(Geo g, int bc_t, int bc_x
 
 void link_phase(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,
                 float2* Wt32, float2* Wx32) {
-  k_link_phase<<<grid_of(g), kBlock, 0, s>>>(g, bc_t, bc_x, A, Wt, Wx, Wt32, Wx32);
+  k_link_phase<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, Wt, Wx, Wt32, Wx32);
 }
 void gauge_step(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double2* A, const double2* mom, double c,
                 int nadd, double2* Wt, double2* Wx, float2* Wt32, float2* Wx32) {
-  k_gauge_step<<<grid_of(g), kBlock, 0, s>>>(g, bc_t, bc_x, A, mom, c, nadd, Wt, Wx, Wt32, Wx32);
+  k_gauge_step<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, mom, c, nadd, Wt, Wx, Wt32, Wx32);
 }
 
 // ---------------------------------------------------------------------------
@@ -72,35 +74,43 @@ void gauge_step(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double2* A, co
 // factors (mu = 0): 18 FMA/MUL per site instead of 22.
 // ---------------------------------------------------------------------------
 template <typename R, int DAG, bool MU0>
-__device__ __forceinline__ C2<R> dslash_site(const OpK<R>& k, const C2<R>* __restrict__ in,
-                                             const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, int s,
-                                             const Nbr& n) {
-  C2<R> v = in[s];
-  C2<R> o = mk<R>(k.m * v.x, k.m * v.y);
+__device__ __forceinline__ C2<R> dslash_vals(const OpK<R>& k, C2<R> pc, C2<R> ptu, C2<R> ptd, C2<R> pxu, C2<R> pxd,
+                                             C2<R> wt, C2<R> wtd, C2<R> wx, C2<R> wxd) {
+  // pc = in(s); ptu/ptd = in(s+t)/in(s-t); pxu/pxd = in(s+x)/in(s-x);
+  // wt = Wt(s), wtd = Wt(s-t), wx = Wx(s), wxd = Wx(s-x)
+  C2<R> o = mk<R>(k.m * pc.x, k.m * pc.y);
   if (MU0) {
     if (DAG == 0) {
-      cmac<R>(o, Wt[s], in[n.tp]);
-      cmsc<R>(o, Wt[n.tm], in[n.tm]);
+      cmac<R>(o, wt, ptu);
+      cmsc<R>(o, wtd, ptd);
     } else {
-      cnmac<R>(o, Wt[s], in[n.tp]);
-      cjmac<R>(o, Wt[n.tm], in[n.tm]);
+      cnmac<R>(o, wt, ptu);
+      cjmac<R>(o, wtd, ptd);
     }
   } else {
-    C2<R> ft = cmul<R>(Wt[s], in[n.tp]);
-    C2<R> bt = cjmul<R>(Wt[n.tm], in[n.tm]);
+    C2<R> ft = cmul<R>(wt, ptu);
+    C2<R> bt = cjmul<R>(wtd, ptd);
     o.x = fma(k.cf, ft.x, o.x);
     o.y = fma(k.cf, ft.y, o.y);
     o.x = fma(k.cb, bt.x, o.x);
     o.y = fma(k.cb, bt.y, o.y);
   }
   if (DAG == 0) {
-    cmac<R>(o, Wx[s], in[n.xp]);
-    cmsc<R>(o, Wx[n.xm], in[n.xm]);
+    cmac<R>(o, wx, pxu);
+    cmsc<R>(o, wxd, pxd);
   } else {
-    cnmac<R>(o, Wx[s], in[n.xp]);
-    cjmac<R>(o, Wx[n.xm], in[n.xm]);
+    cnmac<R>(o, wx, pxu);
+    cjmac<R>(o, wxd, pxd);
   }
   return o;
+}
+
+template <typename R, int DAG, bool MU0>
+__device__ __forceinline__ C2<R> dslash_site(const OpK<R>& k, const C2<R>* __restrict__ in,
+                                             const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, int s,
+                                             const Nbr& n) {
+  return dslash_vals<R, DAG, MU0>(k, in[s], in[n.tp], in[n.tm], in[n.xp], in[n.xm], Wt[s], Wt[n.tm], Wx[s],
+                                  Wx[n.xm]);
 }
 
 template <typename R, int DAG, bool MU0>
@@ -111,11 +121,78 @@ __device__ __forceinline__ C2<R> dslash_at(const Geo& g, const OpK<R>& k, const 
   return dslash_site<R, DAG, MU0>(k, in, Wt, Wx, s, neighbours(g, s, t, x));
 }
 
+template <typename R> __device__ __forceinline__ C2<R> shfl_down1(C2<R> v) {
+  return mk<R>(__shfl_down_sync(0xffffffffu, v.x, 1), __shfl_down_sync(0xffffffffu, v.y, 1));
+}
+template <typename R> __device__ __forceinline__ C2<R> shfl_up1(C2<R> v) {
+  return mk<R>(__shfl_up_sync(0xffffffffu, v.x, 1), __shfl_up_sync(0xffffffffu, v.y, 1));
+}
+
+// One column-march item: rows t0 .. t0+kMarchT-1 of the 32 columns
+// x = 32*xw + lane.  epi(s, out(s), in(s)) consumes each site's result.
+template <typename R, int DAG, bool MU0, class Epi>
+__device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, const C2<R>* __restrict__ in,
+                                           const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, int item,
+                                           Epi& epi) {
+  const int nx = g.nx;
+  const int nxw = nx >> 5;
+  const int tb = item / nxw;
+  const int xw = item - tb * nxw;
+  const int t0 = tb * kMarchT;
+  const int lane = threadIdx.x & 31;
+  const int x = (xw << 5) + lane;
+  const int xr = (x + 1 == nx) ? 0 : x + 1;
+  const int xl = (x == 0) ? nx - 1 : x - 1;
+  const int tm = (t0 == 0) ? g.nt - 1 : t0 - 1;
+  C2<R> pm = in[tm * nx + x];
+  C2<R> wtm = Wt[tm * nx + x];
+  C2<R> pc = in[t0 * nx + x];
+#pragma unroll
+  for (int i = 0; i < kMarchT; i++) {
+    const int t = t0 + i;
+    const int tp = (t + 1 == g.nt) ? 0 : t + 1;
+    const int s = t * nx + x;
+    const C2<R> pp = in[tp * nx + x];
+    const C2<R> wt = Wt[s];
+    const C2<R> wx = Wx[s];
+    C2<R> pr = shfl_down1<R>(pc);
+    C2<R> pl = shfl_up1<R>(pc);
+    C2<R> wl = shfl_up1<R>(wx);
+    if (lane == 31) pr = in[t * nx + xr];
+    if (lane == 0) {
+      pl = in[t * nx + xl];
+      wl = Wx[t * nx + xl];
+    }
+    epi(s, dslash_vals<R, DAG, MU0>(k, pc, pp, pm, pr, pl, wt, wtm, wx, wl), pc);
+    pm = pc;
+    pc = pp;
+    wtm = wt;
+  }
+}
+
+// Apply the operator to every site and hand each result to epi: column march
+// where the lattice allows it, else one site per thread.
+template <typename R, int DAG, bool MU0, class Epi>
+__device__ __forceinline__ void stencil_all(const Geo& g, const OpK<R>& k, const C2<R>* __restrict__ in,
+                                            const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, Epi& epi) {
+  if (g.march) {
+    const int items = (g.nx >> 5) * (g.nt / kMarchT);
+    constexpr int wpb = kBlock / 32;
+    for (int item = blockIdx.x * wpb + (threadIdx.x >> 5); item < items; item += gridDim.x * wpb)
+      march_item<R, DAG, MU0>(g, k, in, Wt, Wx, item, epi);
+  } else {
+    TG_SITES(s, g.V) epi(s, dslash_at<R, DAG, MU0>(g, k, in, Wt, Wx, s), in[s]);
+  }
+}
+
+inline int sgrid(const Geo& g) { return g.march ? g.mgrid : g.grid; }
+
 template <typename R, int DAG, bool MU0>
 __global__ void __launch_bounds__(kBlock) k_dslash(Geo g, OpK<R> k, const C2<R>* __restrict__ in,
                                                    C2<R>* __restrict__ out, const C2<R>* __restrict__ Wt,
                                                    const C2<R>* __restrict__ Wx) {
-  TG_SITES(s, g.V) out[s] = dslash_at<R, DAG, MU0>(g, k, in, Wt, Wx, s);
+  auto epi = [&](int s, C2<R> o, C2<R>) { out[s] = o; };
+  stencil_all<R, DAG, MU0>(g, k, in, Wt, Wx, epi);
 }
 
 // launch helper: picks the MU0 instance from the operator constants
@@ -132,13 +209,13 @@ __global__ void __launch_bounds__(kBlock) k_dslash(Geo g, OpK<R> k, const C2<R>*
 
 void dslash64(cudaStream_t s, const Geo& g, const OpK<double>& k, int dag, const double2* in, double2* out,
               const double2* Wt, const double2* Wx) {
-  if (dag) TG_OP_DISPATCH(k, (k_dslash<double, 1, MU0><<<grid_of(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
-  else TG_OP_DISPATCH(k, (k_dslash<double, 0, MU0><<<grid_of(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
+  if (dag) TG_OP_DISPATCH(k, (k_dslash<double, 1, MU0><<<sgrid(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
+  else TG_OP_DISPATCH(k, (k_dslash<double, 0, MU0><<<sgrid(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
 }
 void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, int dag, const float2* in, float2* out,
               const float2* Wt, const float2* Wx) {
-  if (dag) TG_OP_DISPATCH(k, (k_dslash<float, 1, MU0><<<grid_of(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
-  else TG_OP_DISPATCH(k, (k_dslash<float, 0, MU0><<<grid_of(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
+  if (dag) TG_OP_DISPATCH(k, (k_dslash<float, 1, MU0><<<sgrid(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
+  else TG_OP_DISPATCH(k, (k_dslash<float, 0, MU0><<<sgrid(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
 }
 
 // ---------------------------------------------------------------------------
@@ -213,12 +290,12 @@ __global__ void __launch_bounds__(kBlock) k_cg1(Geo g, OpK<R> k, const C2<R>* __
                                                 CgState* st, Red red) {
   if (st->done) return;
   R v = 0;
-  TG_SITES(s, g.V) {
-    C2<R> o = dslash_at<R, 0, MU0>(g, k, p, Wt, Wx, s);
+  auto epi = [&](int s, C2<R> o, C2<R>) {
     Mp[s] = o;
     v = fma(o.x, o.x, v);
     v = fma(o.y, o.y, v);
-  }
+  };
+  stencil_all<R, 0, MU0>(g, k, p, Wt, Wx, epi);
   double tot;
   if (grid_sum<kBlock, R>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) {
     st->alpha = st->rr / tot;
@@ -237,8 +314,7 @@ __global__ void __launch_bounds__(kBlock) k_cg2_64(Geo g, OpK<double> k, const d
   if (st->done) return;
   const double a = st->alpha;
   double v = 0;
-  TG_SITES(s, g.V) {
-    double2 ap = dslash_at<double, 1, MU0>(g, k, Mp, Wt, Wx, s);
+  auto epi = [&](int s, double2 ap, double2) {
     double2 xv = x[s], pv = p[s], rv = r[s];
     xv.x += a * pv.x;
     xv.y += a * pv.y;
@@ -248,7 +324,8 @@ __global__ void __launch_bounds__(kBlock) k_cg2_64(Geo g, OpK<double> k, const d
     r[s] = rv;
     v = fma(rv.x, rv.x, v);
     v = fma(rv.y, rv.y, v);
-  }
+  };
+  stencil_all<double, 1, MU0>(g, k, Mp, Wt, Wx, epi);
   double rn;
   if (grid_sum<kBlock, double>(v, red.partials, red.counter, &rn) && threadIdx.x == 0) {
     st->iter += 1;
@@ -281,10 +358,9 @@ void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const
 
 void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
                double2* x, const CgBufs64& w, CgState* st, CgLog* log, const Red& red, Cond c) {
-  const int nb = grid_of(g);
-  TG_OP_DISPATCH(km, (k_cg1<double, MU0><<<nb, kBlock, 0, s>>>(g, km, w.p, w.Mp, L.Wt, L.Wx, st, red)));
-  TG_OP_DISPATCH(kd, (k_cg2_64<MU0><<<nb, kBlock, 0, s>>>(g, kd, w.Mp, w.p, x, w.r, L.Wt, L.Wx, st, log, red, c)));
-  k_cg3<double><<<nb, kBlock, 0, s>>>(g.V, w.r, w.p, st);
+  TG_OP_DISPATCH(km, (k_cg1<double, MU0><<<sgrid(g), kBlock, 0, s>>>(g, km, w.p, w.Mp, L.Wt, L.Wx, st, red)));
+  TG_OP_DISPATCH(kd, (k_cg2_64<MU0><<<sgrid(g), kBlock, 0, s>>>(g, kd, w.Mp, w.p, x, w.r, L.Wt, L.Wx, st, log, red, c)));
+  k_cg3<double><<<stream_grid(g.V), kBlock, 0, s>>>(g.V, w.r, w.p, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -302,8 +378,7 @@ __global__ void __launch_bounds__(kBlock) k_cgmx2(Geo g, OpK<float> k, const flo
   if (st->done) return;
   const float a = (float)st->alpha;
   float v = 0;
-  TG_SITES(s, g.V) {
-    float2 ap = dslash_at<float, 1, MU0>(g, k, Mp, Wt, Wx, s);
+  auto epi = [&](int s, float2 ap, float2) {
     float2 xv = xs[s], pv = p[s], rv = r[s];
     xv.x = fmaf(a, pv.x, xv.x);
     xv.y = fmaf(a, pv.y, xv.y);
@@ -313,7 +388,8 @@ __global__ void __launch_bounds__(kBlock) k_cgmx2(Geo g, OpK<float> k, const flo
     r[s] = rv;
     v = fmaf(rv.x, rv.x, v);
     v = fmaf(rv.y, rv.y, v);
-  }
+  };
+  stencil_all<float, 1, MU0>(g, k, Mp, Wt, Wx, epi);
   double rn;
   if (grid_sum<kBlock, float>(v, red.partials, red.counter, &rn) && threadIdx.x == 0) {
     st->iter += 1;
@@ -347,7 +423,8 @@ __global__ void __launch_bounds__(kBlock) k_ru2(Geo g, OpK<double> k, const doub
                                                 double2* __restrict__ tmp, const double2* __restrict__ Wt,
                                                 const double2* __restrict__ Wx, const CgState* st) {
   if (!st->need_ru || st->done) return;
-  TG_SITES(s, g.V) tmp[s] = dslash_at<double, 0, MU0>(g, k, x, Wt, Wx, s);
+  auto epi = [&](int s, double2 o, double2) { tmp[s] = o; };
+  stencil_all<double, 0, MU0>(g, k, x, Wt, Wx, epi);
 }
 
 // reliable update 3: r = b - M^dag tmp (FP64), rs = (float) r, decide
@@ -358,14 +435,14 @@ __global__ void __launch_bounds__(kBlock) k_ru3(Geo g, OpK<double> k, const doub
                                                 CgState* st, CgLog* log, Red red, Cond c) {
   if (!st->need_ru || st->done) return;
   double v = 0;
-  TG_SITES(s, g.V) {
-    double2 ap = dslash_at<double, 1, MU0>(g, k, tmp, Wt, Wx, s);
+  auto epi = [&](int s, double2 ap, double2) {
     double2 bb = b[s];
     double2 rv = make_double2(bb.x - ap.x, bb.y - ap.y);
     rs[s] = make_float2((float)rv.x, (float)rv.y);
     v = fma(rv.x, rv.x, v);
     v = fma(rv.y, rv.y, v);
-  }
+  };
+  stencil_all<double, 1, MU0>(g, k, tmp, Wt, Wx, epi);
   double rt;
   if (grid_sum<kBlock, double>(v, red.partials, red.counter, &rt) && threadIdx.x == 0) {
     st->restart = rt > kRuRestart * st->rr;  // recursive residual was far too optimistic
@@ -396,21 +473,19 @@ void cgmx_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const
 
 void cgmx_iter(cudaStream_t s, const Geo& g, const OpK<float>& km, const OpK<float>& kd, const Links& L,
                const CgBufsMixed& w, CgState* st, const Red& red, Cond c) {
-  const int nb = grid_of(g);
-  TG_OP_DISPATCH(km, (k_cg1<float, MU0><<<nb, kBlock, 0, s>>>(g, km, w.ps, w.Mps, L.Wt32, L.Wx32, st, red)));
+  TG_OP_DISPATCH(km, (k_cg1<float, MU0><<<sgrid(g), kBlock, 0, s>>>(g, km, w.ps, w.Mps, L.Wt32, L.Wx32, st, red)));
   TG_OP_DISPATCH(kd,
-                 (k_cgmx2<MU0><<<nb, kBlock, 0, s>>>(g, kd, w.Mps, w.ps, w.xs, w.rs, L.Wt32, L.Wx32, st, red, c)));
-  k_cg3<float><<<nb, kBlock, 0, s>>>(g.V, w.rs, w.ps, st);
+                 (k_cgmx2<MU0><<<sgrid(g), kBlock, 0, s>>>(g, kd, w.Mps, w.ps, w.xs, w.rs, L.Wt32, L.Wx32, st, red, c)));
+  k_cg3<float><<<stream_grid(g.V), kBlock, 0, s>>>(g.V, w.rs, w.ps, st);
 }
 
 void cgmx_reliable(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
                    const double2* b, double2* x, const CgBufsMixed& w, CgState* st, CgLog* log, const Red& red,
                    Cond c) {
-  const int nb = grid_of(g);
-  k_ru1<<<nb, kBlock, 0, s>>>(g.V, x, w.xs, st);
-  TG_OP_DISPATCH(km, (k_ru2<MU0><<<nb, kBlock, 0, s>>>(g, km, x, w.tmp64, L.Wt, L.Wx, st)));
-  TG_OP_DISPATCH(kd, (k_ru3<MU0><<<nb, kBlock, 0, s>>>(g, kd, b, w.tmp64, w.rs, L.Wt, L.Wx, st, log, red, c)));
-  k_ru4<<<nb, kBlock, 0, s>>>(g.V, w.rs, w.ps, st);
+  k_ru1<<<stream_grid(g.V), kBlock, 0, s>>>(g.V, x, w.xs, st);
+  TG_OP_DISPATCH(km, (k_ru2<MU0><<<sgrid(g), kBlock, 0, s>>>(g, km, x, w.tmp64, L.Wt, L.Wx, st)));
+  TG_OP_DISPATCH(kd, (k_ru3<MU0><<<sgrid(g), kBlock, 0, s>>>(g, kd, b, w.tmp64, w.rs, L.Wt, L.Wx, st, log, red, c)));
+  k_ru4<<<stream_grid(g.V), kBlock, 0, s>>>(g.V, w.rs, w.ps, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -456,11 +531,8 @@ __global__ void __launch_bounds__(kBlock) k_md_action(Geo g, OpK<double> k, cons
                                                       const double2* __restrict__ Wt, const double2* __restrict__ Wx,
                                                       double* dst, Red red) {
   double a = 0;
-  TG_SITES(s, g.V) {
-    double2 o = dslash_at<double, 1, MU0>(g, k, nz, Wt, Wx, s);
-    double2 v = nz[s];
-    a += v.x * o.x + v.y * o.y;
-  }
+  auto epi = [&](int, double2 o, double2 v) { a += v.x * o.x + v.y * o.y; };
+  stencil_all<double, 1, MU0>(g, k, nz, Wt, Wx, epi);
   double tot;
   if (grid_sum<kBlock, double>(a, red.partials, red.counter, &tot) && threadIdx.x == 0) *dst = tot;
 }
@@ -477,7 +549,7 @@ void gauge_action(cudaStream_t s, const Geo& g, const double2* A, double fac, do
 }
 void md_action(cudaStream_t s, const Geo& g, const OpK<double>& kd, const double2* nz, const double2* Wt,
                const double2* Wx, double* dst, const Red& red) {
-  TG_OP_DISPATCH(kd, (k_md_action<MU0><<<grid_of(g), kBlock, 0, s>>>(g, kd, nz, Wt, Wx, dst, red)));
+  TG_OP_DISPATCH(kd, (k_md_action<MU0><<<sgrid(g), kBlock, 0, s>>>(g, kd, nz, Wt, Wx, dst, red)));
 }
 
 // ---------------------------------------------------------------------------
@@ -573,12 +645,12 @@ __global__ void __launch_bounds__(kBlock) k_force_field(Geo g, double ep, double
 void momentum_update(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
                      const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise,
                      double2* mom, double eps, double gfac, int flags) {
-  k_momentum_update<<<grid_of(g), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, mom, eps, gfac, flags);
+  k_momentum_update<<<stream_grid(g.V), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, mom, eps, gfac, flags);
 }
 void force_field(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
                  const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise, double2* F,
                  double gfac, int flags) {
-  k_force_field<<<grid_of(g), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, F, gfac, flags);
+  k_force_field<<<stream_grid(g.V), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, F, gfac, flags);
 }
 
 // ---------------------------------------------------------------------------
@@ -627,7 +699,7 @@ __global__ void k_philox_uniform(unsigned long long seed, TrajStats* ts, unsigne
 
 void philox_gauss(cudaStream_t s, const Geo& g, unsigned long long seed, const TrajStats* ts, unsigned stream_id,
                   double2* out) {
-  k_philox_gauss<<<grid_of(g), kBlock, 0, s>>>(g.V, seed, ts, stream_id, out);
+  k_philox_gauss<<<stream_grid(g.V), kBlock, 0, s>>>(g.V, seed, ts, stream_id, out);
 }
 void philox_uniform(cudaStream_t s, unsigned long long seed, TrajStats* ts, unsigned stream_id) {
   k_philox_uniform<<<1, 1, 0, s>>>(seed, ts, stream_id);
@@ -649,7 +721,7 @@ __global__ void __launch_bounds__(kBlock) k_puregauge(int n, double* A, const do
 }
 
 void puregauge(cudaStream_t s, const Geo& g, double* A, const double* u, double c) {
-  k_puregauge<<<grid_of(g), kBlock, 0, s>>>(2 * g.V, A, u, c);
+  k_puregauge<<<stream_grid(2 * g.V), kBlock, 0, s>>>(2 * g.V, A, u, c);
 }
 
 // dH in the order of hmc.c:729-732, accept if exp(-dH) > u (hmc.c:738)
@@ -668,7 +740,7 @@ __global__ void __launch_bounds__(kBlock) k_accept_copy(int n, const TrajStats* 
 
 void finish_trajectory(cudaStream_t s, TrajStats* ts) { k_finish<<<1, 1, 0, s>>>(ts); }
 void accept_copy(cudaStream_t s, const Geo& g, const TrajStats* ts, double2* A, const double2* Anew) {
-  k_accept_copy<<<grid_of(g), kBlock, 0, s>>>(g.V, ts, A, Anew);
+  k_accept_copy<<<stream_grid(g.V), kBlock, 0, s>>>(g.V, ts, A, Anew);
 }
 
 }  // namespace tg
