@@ -248,21 +248,25 @@ int enqueue_cg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const doub
     TG_CK(cudaGetLastError());
     cudaGraph_t body;
     TG_TRY(add_conditional(s, hloop, cudaGraphCondTypeWhile, &body));
+    // the body holds two iterations (p alternates between its two buffers);
+    // the kernels of the second are no-ops once the first has converged
     TG_CK(cudaStreamBeginCaptureToGraph(L->cap2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    if (!mixed) {
-      cg64_iter(L->cap2, g, km, kd, lk, x, L->w64, L->st, L->log, L->red, c0);
-    } else {
-      cudaGraphConditionalHandle hru;
-      TG_CK(cudaGraphConditionalHandleCreate(&hru, body, 0, 0));
-      Cond c1{hloop, hru, 1};
-      cgmx_iter(L->cap2, g, km32, kd32, lk, L->wmx, L->st, L->red, c1);
-      cudaGraph_t ifbody;
-      TG_TRY(add_conditional(L->cap2, hru, cudaGraphCondTypeIf, &ifbody));
-      TG_CK(cudaStreamBeginCaptureToGraph(L->cap3, ifbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-      cgmx_reliable(L->cap3, g, km, kd, lk, b, x, L->wmx, L->st, L->log, L->red, c1);
-      TG_CK(cudaGetLastError());
-      cudaGraph_t tmp;
-      TG_CK(cudaStreamEndCapture(L->cap3, &tmp));
+    for (int half = 0; half < 2; half++) {
+      if (!mixed) {
+        cg64_iter(L->cap2, g, km, kd, lk, x, L->w64, half, L->st, L->log, L->red, c0);
+      } else {
+        cudaGraphConditionalHandle hru;
+        TG_CK(cudaGraphConditionalHandleCreate(&hru, body, 0, 0));
+        Cond c1{hloop, hru, 1};
+        cgmx_iter(L->cap2, g, km32, kd32, lk, L->wmx, half, L->st, L->red, c1);
+        cudaGraph_t ifbody;
+        TG_TRY(add_conditional(L->cap2, hru, cudaGraphCondTypeIf, &ifbody));
+        TG_CK(cudaStreamBeginCaptureToGraph(L->cap3, ifbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+        cgmx_reliable(L->cap3, g, km, kd, lk, b, x, L->wmx, L->st, L->log, L->red, c1);
+        TG_CK(cudaGetLastError());
+        cudaGraph_t tmp;
+        TG_CK(cudaStreamEndCapture(L->cap3, &tmp));
+      }
     }
     TG_CK(cudaGetLastError());
     cudaGraph_t tmp;
@@ -282,11 +286,12 @@ int enqueue_cg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const doub
     TG_CK(cudaMemcpyAsync(L->h_st, L->st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
     TG_CK(cudaStreamSynchronize(s));
     if (L->h_st->done) return TG_OK;
-    for (int j = 0; j < chunk; j++) {
+    for (int j = 0; j < chunk; j++) {  // chunk is even: p ends in buffer 0 again
+      const int half = j & 1;
       if (!mixed) {
-        cg64_iter(s, g, km, kd, lk, x, L->w64, L->st, L->log, L->red, none);
+        cg64_iter(s, g, km, kd, lk, x, L->w64, half, L->st, L->log, L->red, none);
       } else {
-        cgmx_iter(s, g, km32, kd32, lk, L->wmx, L->st, L->red, none);
+        cgmx_iter(s, g, km32, kd32, lk, L->wmx, half, L->st, L->red, none);
         cgmx_reliable(s, g, km, kd, lk, b, x, L->wmx, L->st, L->log, L->red, none);
       }
     }
@@ -550,10 +555,10 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
   size_t n = (size_t)V;
   int rc = TG_OK;
   double2** d2[] = {&L->A, &L->Anew, &L->Wt, &L->Wx, &L->mom, &L->noise, &L->chi, &L->Mchi, &L->vin, &L->vout,
-                    &L->w64.r, &L->w64.p, &L->w64.Mp, &L->wmx.tmp64};
+                    &L->w64.r, &L->w64.p[0], &L->w64.p[1], &L->w64.Mp, &L->wmx.tmp64};
   for (auto pp : d2)
     if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
-  float2** f2[] = {&L->Wt32, &L->Wx32, &L->wmx.xs, &L->wmx.rs, &L->wmx.ps, &L->wmx.Mps};
+  float2** f2[] = {&L->Wt32, &L->Wx32, &L->wmx.xs, &L->wmx.rs, &L->wmx.ps[0], &L->wmx.ps[1], &L->wmx.Mps};
   for (auto pp : f2)
     if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
   if ((rc = dmalloc(&L->st, 1)) != TG_OK || (rc = dmalloc(&L->log, kMaxLog)) != TG_OK ||
@@ -591,7 +596,8 @@ int tg_destroy(tg_lattice* L) {
   }
   for (auto e : L->ev) cudaEventDestroy(e);
   void* dev[] = {L->A, L->Anew, L->Wt, L->Wx, L->mom, L->noise, L->chi, L->Mchi, L->vin, L->vout, L->w64.r,
-                 L->w64.p, L->w64.Mp, L->wmx.tmp64, L->Wt32, L->Wx32, L->wmx.xs, L->wmx.rs, L->wmx.ps, L->wmx.Mps,
+                 L->w64.p[0], L->w64.p[1], L->w64.Mp, L->wmx.tmp64, L->Wt32, L->Wx32, L->wmx.xs, L->wmx.rs,
+                 L->wmx.ps[0], L->wmx.ps[1], L->wmx.Mps,
                  L->st, L->log, L->ts, L->red.partials, L->red.counter, L->eta, L->phi, L->unif};
   for (void* d : dev)
     if (d) cudaFree(d);
@@ -682,8 +688,8 @@ int tg_time_apply(tg_lattice* L, int n, int dagger, int precision, double* ms_pe
       double2* out = (i & 1) ? L->vin : L->vout;
       dslash64(L->stream, L->g, op_k(L, dagger), dagger, in, out, L->Wt, L->Wx);
     } else {
-      const float2* in = (i & 1) ? L->wmx.Mps : L->wmx.ps;
-      float2* out = (i & 1) ? L->wmx.ps : L->wmx.Mps;
+      const float2* in = (i & 1) ? L->wmx.Mps : L->wmx.ps[0];
+      float2* out = (i & 1) ? L->wmx.ps[0] : L->wmx.Mps;
       dslash32(L->stream, L->g, op_k32(L, dagger), dagger, in, out, L->Wt32, L->Wx32);
     }
   }

@@ -11,6 +11,9 @@
 // results do not depend on block scheduling.
 #include <math.h>
 
+#include <mutex>
+#include <unordered_map>
+
 #include "tg_launch.h"
 
 namespace tg {
@@ -129,11 +132,12 @@ template <typename R> __device__ __forceinline__ C2<R> shfl_up1(C2<R> v) {
 }
 
 // One column-march item: rows t0 .. t0+kMarchT-1 of the 32 columns
-// x = 32*xw + lane.  epi(s, out(s), in(s)) consumes each site's result.
-template <typename R, int DAG, bool MU0, class Epi>
-__device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, const C2<R>* __restrict__ in,
-                                           const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, int item,
-                                           Epi& epi) {
+// x = 32*xw + lane.  ld(i) yields the operand at site i (a plain load, or a
+// vector recombined on the fly); epi(s, out(s), operand(s)) consumes each
+// site's result.
+template <typename R, int DAG, bool MU0, class Ld, class Epi>
+__device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
+                                           const C2<R>* __restrict__ Wx, int item, Epi& epi) {
   const int nx = g.nx;
   const int nxw = nx >> 5;
   const int tb = item / nxw;
@@ -144,23 +148,23 @@ __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, const 
   const int xr = (x + 1 == nx) ? 0 : x + 1;
   const int xl = (x == 0) ? nx - 1 : x - 1;
   const int tm = (t0 == 0) ? g.nt - 1 : t0 - 1;
-  C2<R> pm = in[tm * nx + x];
+  C2<R> pm = ld(tm * nx + x);
   C2<R> wtm = Wt[tm * nx + x];
-  C2<R> pc = in[t0 * nx + x];
+  C2<R> pc = ld(t0 * nx + x);
 #pragma unroll
   for (int i = 0; i < kMarchT; i++) {
     const int t = t0 + i;
     const int tp = (t + 1 == g.nt) ? 0 : t + 1;
     const int s = t * nx + x;
-    const C2<R> pp = in[tp * nx + x];
+    const C2<R> pp = ld(tp * nx + x);
     const C2<R> wt = Wt[s];
     const C2<R> wx = Wx[s];
     C2<R> pr = shfl_down1<R>(pc);
     C2<R> pl = shfl_up1<R>(pc);
     C2<R> wl = shfl_up1<R>(wx);
-    if (lane == 31) pr = in[t * nx + xr];
+    if (lane == 31) pr = ld(t * nx + xr);
     if (lane == 0) {
-      pl = in[t * nx + xl];
+      pl = ld(t * nx + xl);
       wl = Wx[t * nx + xl];
     }
     epi(s, dslash_vals<R, DAG, MU0>(k, pc, pp, pm, pr, pl, wt, wtm, wx, wl), pc);
@@ -172,20 +176,63 @@ __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, const 
 
 // Apply the operator to every site and hand each result to epi: column march
 // where the lattice allows it, else one site per thread.
-template <typename R, int DAG, bool MU0, class Epi>
-__device__ __forceinline__ void stencil_all(const Geo& g, const OpK<R>& k, const C2<R>* __restrict__ in,
-                                            const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, Epi& epi) {
+template <typename R, int DAG, bool MU0, class Ld, class Epi>
+__device__ __forceinline__ void stencil_ld(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
+                                           const C2<R>* __restrict__ Wx, Epi& epi) {
   if (g.march) {
     const int items = (g.nx >> 5) * (g.nt / kMarchT);
     constexpr int wpb = kBlock / 32;
     for (int item = blockIdx.x * wpb + (threadIdx.x >> 5); item < items; item += gridDim.x * wpb)
-      march_item<R, DAG, MU0>(g, k, in, Wt, Wx, item, epi);
+      march_item<R, DAG, MU0>(g, k, ld, Wt, Wx, item, epi);
   } else {
-    TG_SITES(s, g.V) epi(s, dslash_at<R, DAG, MU0>(g, k, in, Wt, Wx, s), in[s]);
+    TG_SITES(s, g.V) {
+      int t, x;
+      site_tx(g, s, t, x);
+      const Nbr n = neighbours(g, s, t, x);
+      const C2<R> pc = ld(s);
+      epi(s, dslash_vals<R, DAG, MU0>(k, pc, ld(n.tp), ld(n.tm), ld(n.xp), ld(n.xm), Wt[s], Wt[n.tm], Wx[s],
+                                      Wx[n.xm]),
+          pc);
+    }
   }
 }
 
-inline int sgrid(const Geo& g) { return g.march ? g.mgrid : g.grid; }
+template <typename R, int DAG, bool MU0, class Epi>
+__device__ __forceinline__ void stencil_all(const Geo& g, const OpK<R>& k, const C2<R>* __restrict__ in,
+                                            const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, Epi& epi) {
+  auto ld = [&](int i) { return in[i]; };
+  stencil_ld<R, DAG, MU0>(g, k, ld, Wt, Wx, epi);
+}
+
+// Blocks of work of a stencil kernel (march: 8 warp items per block).
+inline int stencil_work(const Geo& g) {
+  return g.march ? ((g.nx >> 5) * (g.nt / kMarchT) + kBlock / 32 - 1) / (kBlock / 32) : nblocks(g.V);
+}
+
+// Grid = resident blocks of this kernel on the GPU (one wave), at most `work`.
+template <class K> int occ_grid(K kernel, int work) {
+  static int sms = 0;
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+  }
+  auto it = cache.find((const void*)kernel);
+  int per_sm;
+  if (it == cache.end()) {
+    per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm <= 0)
+      per_sm = 1;
+    cache.emplace((const void*)kernel, per_sm);
+  } else {
+    per_sm = it->second;
+  }
+  int grid = per_sm * sms;
+  return grid < work ? grid : (work > 0 ? work : 1);
+}
 
 template <typename R, int DAG, bool MU0>
 __global__ void __launch_bounds__(kBlock) k_dslash(Geo g, OpK<R> k, const C2<R>* __restrict__ in,
@@ -209,20 +256,33 @@ __global__ void __launch_bounds__(kBlock) k_dslash(Geo g, OpK<R> k, const C2<R>*
 
 void dslash64(cudaStream_t s, const Geo& g, const OpK<double>& k, int dag, const double2* in, double2* out,
               const double2* Wt, const double2* Wx) {
-  if (dag) TG_OP_DISPATCH(k, (k_dslash<double, 1, MU0><<<sgrid(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
-  else TG_OP_DISPATCH(k, (k_dslash<double, 0, MU0><<<sgrid(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
+  const int w = stencil_work(g);
+  if (dag)
+    TG_OP_DISPATCH(k, (k_dslash<double, 1, MU0><<<occ_grid(k_dslash<double, 1, MU0>, w), kBlock, 0, s>>>(
+                          g, k, in, out, Wt, Wx)));
+  else
+    TG_OP_DISPATCH(k, (k_dslash<double, 0, MU0><<<occ_grid(k_dslash<double, 0, MU0>, w), kBlock, 0, s>>>(
+                          g, k, in, out, Wt, Wx)));
 }
 void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, int dag, const float2* in, float2* out,
               const float2* Wt, const float2* Wx) {
-  if (dag) TG_OP_DISPATCH(k, (k_dslash<float, 1, MU0><<<sgrid(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
-  else TG_OP_DISPATCH(k, (k_dslash<float, 0, MU0><<<sgrid(g), kBlock, 0, s>>>(g, k, in, out, Wt, Wx)));
+  const int w = stencil_work(g);
+  if (dag)
+    TG_OP_DISPATCH(k, (k_dslash<float, 1, MU0><<<occ_grid(k_dslash<float, 1, MU0>, w), kBlock, 0, s>>>(
+                          g, k, in, out, Wt, Wx)));
+  else
+    TG_OP_DISPATCH(k, (k_dslash<float, 0, MU0><<<occ_grid(k_dslash<float, 0, MU0>, w), kBlock, 0, s>>>(
+                          g, k, in, out, Wt, Wx)));
 }
 
 // ---------------------------------------------------------------------------
 // CG on M^dagger M (fmdm_invert_cg, hmc.c:341-404), one iteration =
-//   K1: Mp = M p,  pAp = |Mp|^2,            alpha = rr / pAp
-//   K2: x += alpha p, r -= alpha M^dag Mp,  rr' = |r|^2, beta = rr'/rr, tests
-//   K3: p = r + beta p
+//   K1: p' = r + beta p (formed on the fly for every operand the stencil
+//       reads, stored at the own site), Mp = M p', pAp = |Mp|^2, alpha = rr/pAp
+//   K2: x += alpha p', r -= alpha M^dag Mp, rr' = |r|^2, beta = rr'/rr, tests
+// so the p update costs no pass of its own.  p lives in two buffers that
+// alternate between consecutive iterations (p' cannot overwrite p while
+// neighbouring sites still read it); the graph body holds two iterations.
 // pAp = <p, M^dag M p> is taken as |Mp|^2 (same value, always >= 0).  The
 // scalar recurrences run in the last block of K1/K2, so the host never waits.
 // The FP32 instances (mixed precision) accumulate per-block sums in FP32 and
@@ -285,17 +345,24 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(Geo g, const double2* __rest
 }
 
 template <typename R, bool MU0>
-__global__ void __launch_bounds__(kBlock) k_cg1(Geo g, OpK<R> k, const C2<R>* __restrict__ p, C2<R>* __restrict__ Mp,
-                                                const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx,
-                                                CgState* st, Red red) {
+__global__ void __launch_bounds__(kBlock) k_cg1(Geo g, OpK<R> k, const C2<R>* __restrict__ r,
+                                                const C2<R>* __restrict__ p_old, C2<R>* __restrict__ p_new,
+                                                C2<R>* __restrict__ Mp, const C2<R>* __restrict__ Wt,
+                                                const C2<R>* __restrict__ Wx, CgState* st, Red red) {
   if (st->done) return;
+  const R b = (R)st->beta;
   R v = 0;
-  auto epi = [&](int s, C2<R> o, C2<R>) {
+  auto ld = [&](int i) {
+    const C2<R> rv = r[i], pv = p_old[i];
+    return mk<R>(fma(b, pv.x, rv.x), fma(b, pv.y, rv.y));
+  };
+  auto epi = [&](int s, C2<R> o, C2<R> pc) {
+    p_new[s] = pc;
     Mp[s] = o;
     v = fma(o.x, o.x, v);
     v = fma(o.y, o.y, v);
   };
-  stencil_all<R, 0, MU0>(g, k, p, Wt, Wx, epi);
+  stencil_ld<R, 0, MU0>(g, k, ld, Wt, Wx, epi);
   double tot;
   if (grid_sum<kBlock, R>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) {
     st->alpha = st->rr / tot;
@@ -339,28 +406,21 @@ __global__ void __launch_bounds__(kBlock) k_cg2_64(Geo g, OpK<double> k, const d
   }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(kBlock) k_cg3(int n, const C2<R>* __restrict__ r, C2<R>* __restrict__ p,
-                                                const CgState* st) {
-  if (st->done) return;
-  const R b = (R)st->beta;
-  TG_SITES(s, n) {
-    C2<R> rv = r[s], pv = p[s];
-    p[s] = mk<R>(fma(b, pv.x, rv.x), fma(b, pv.y, rv.y));
-  }
-}
-
 void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
                CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int log_index, Cond c) {
-  k_cg_init<double><<<grid_of(g), kBlock, 0, s>>>(g, b, x, w.r, w.p, nullptr, rel_tol, abs_tol2, maxiter, 0,
-                                                  log_index, st, log, red, c);
+  k_cg_init<double><<<occ_grid(k_cg_init<double>, nblocks(g.V)), kBlock, 0, s>>>(
+      g, b, x, w.r, w.p[0], nullptr, rel_tol, abs_tol2, maxiter, 0, log_index, st, log, red, c);
 }
 
 void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
-               double2* x, const CgBufs64& w, CgState* st, CgLog* log, const Red& red, Cond c) {
-  TG_OP_DISPATCH(km, (k_cg1<double, MU0><<<sgrid(g), kBlock, 0, s>>>(g, km, w.p, w.Mp, L.Wt, L.Wx, st, red)));
-  TG_OP_DISPATCH(kd, (k_cg2_64<MU0><<<sgrid(g), kBlock, 0, s>>>(g, kd, w.Mp, w.p, x, w.r, L.Wt, L.Wx, st, log, red, c)));
-  k_cg3<double><<<stream_grid(g.V), kBlock, 0, s>>>(g.V, w.r, w.p, st);
+               double2* x, const CgBufs64& w, int half, CgState* st, CgLog* log, const Red& red, Cond c) {
+  const int wk = stencil_work(g);
+  const double2* p_old = w.p[half];
+  double2* p_new = w.p[half ^ 1];
+  TG_OP_DISPATCH(km, (k_cg1<double, MU0><<<occ_grid(k_cg1<double, MU0>, wk), kBlock, 0, s>>>(
+                          g, km, w.r, p_old, p_new, w.Mp, L.Wt, L.Wx, st, red)));
+  TG_OP_DISPATCH(kd, (k_cg2_64<MU0><<<occ_grid(k_cg2_64<MU0>, wk), kBlock, 0, s>>>(g, kd, w.Mp, p_new, x, w.r, L.Wt,
+                                                                                 L.Wx, st, log, red, c)));
 }
 
 // ---------------------------------------------------------------------------
@@ -445,7 +505,8 @@ __global__ void __launch_bounds__(kBlock) k_ru3(Geo g, OpK<double> k, const doub
   stencil_all<double, 1, MU0>(g, k, tmp, Wt, Wx, epi);
   double rt;
   if (grid_sum<kBlock, double>(v, red.partials, red.counter, &rt) && threadIdx.x == 0) {
-    st->restart = rt > kRuRestart * st->rr;  // recursive residual was far too optimistic
+    st->restart = rt > kRuRestart * st->rr;  // recursive residual was far too optimistic:
+    if (st->restart) st->beta = 0;            // the next p starts again from r
     st->rr_true = rt;
     st->rr = rt;
     st->since_ru = 0;
@@ -457,35 +518,32 @@ __global__ void __launch_bounds__(kBlock) k_ru3(Geo g, OpK<double> k, const doub
   }
 }
 
-// reliable update 4: restart the search direction from the new residual
-__global__ void __launch_bounds__(kBlock) k_ru4(int n, const float2* __restrict__ rs, float2* __restrict__ ps,
-                                                const CgState* st) {
-  if (!st->need_ru || !st->restart || st->done) return;
-  TG_SITES(s, n) ps[s] = rs[s];
-}
-
 void cgmx_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufsMixed& w, CgState* st,
                CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int ru_interval,
                int log_index, Cond c) {
-  k_cg_init<float><<<grid_of(g), kBlock, 0, s>>>(g, b, x, w.rs, w.ps, w.xs, rel_tol, abs_tol2, maxiter,
-                                                 ru_interval, log_index, st, log, red, c);
+  k_cg_init<float><<<occ_grid(k_cg_init<float>, nblocks(g.V)), kBlock, 0, s>>>(
+      g, b, x, w.rs, w.ps[0], w.xs, rel_tol, abs_tol2, maxiter, ru_interval, log_index, st, log, red, c);
 }
 
 void cgmx_iter(cudaStream_t s, const Geo& g, const OpK<float>& km, const OpK<float>& kd, const Links& L,
-               const CgBufsMixed& w, CgState* st, const Red& red, Cond c) {
-  TG_OP_DISPATCH(km, (k_cg1<float, MU0><<<sgrid(g), kBlock, 0, s>>>(g, km, w.ps, w.Mps, L.Wt32, L.Wx32, st, red)));
-  TG_OP_DISPATCH(kd,
-                 (k_cgmx2<MU0><<<sgrid(g), kBlock, 0, s>>>(g, kd, w.Mps, w.ps, w.xs, w.rs, L.Wt32, L.Wx32, st, red, c)));
-  k_cg3<float><<<stream_grid(g.V), kBlock, 0, s>>>(g.V, w.rs, w.ps, st);
+               const CgBufsMixed& w, int half, CgState* st, const Red& red, Cond c) {
+  const int wk = stencil_work(g);
+  const float2* p_old = w.ps[half];
+  float2* p_new = w.ps[half ^ 1];
+  TG_OP_DISPATCH(km, (k_cg1<float, MU0><<<occ_grid(k_cg1<float, MU0>, wk), kBlock, 0, s>>>(
+                          g, km, w.rs, p_old, p_new, w.Mps, L.Wt32, L.Wx32, st, red)));
+  TG_OP_DISPATCH(kd, (k_cgmx2<MU0><<<occ_grid(k_cgmx2<MU0>, wk), kBlock, 0, s>>>(g, kd, w.Mps, p_new, w.xs, w.rs,
+                                                                               L.Wt32, L.Wx32, st, red, c)));
 }
 
 void cgmx_reliable(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
                    const double2* b, double2* x, const CgBufsMixed& w, CgState* st, CgLog* log, const Red& red,
                    Cond c) {
+  const int wk = stencil_work(g);
   k_ru1<<<stream_grid(g.V), kBlock, 0, s>>>(g.V, x, w.xs, st);
-  TG_OP_DISPATCH(km, (k_ru2<MU0><<<sgrid(g), kBlock, 0, s>>>(g, km, x, w.tmp64, L.Wt, L.Wx, st)));
-  TG_OP_DISPATCH(kd, (k_ru3<MU0><<<sgrid(g), kBlock, 0, s>>>(g, kd, b, w.tmp64, w.rs, L.Wt, L.Wx, st, log, red, c)));
-  k_ru4<<<stream_grid(g.V), kBlock, 0, s>>>(g.V, w.rs, w.ps, st);
+  TG_OP_DISPATCH(km, (k_ru2<MU0><<<occ_grid(k_ru2<MU0>, wk), kBlock, 0, s>>>(g, km, x, w.tmp64, L.Wt, L.Wx, st)));
+  TG_OP_DISPATCH(kd, (k_ru3<MU0><<<occ_grid(k_ru3<MU0>, wk), kBlock, 0, s>>>(g, kd, b, w.tmp64, w.rs, L.Wt, L.Wx, st,
+                                                                           log, red, c)));
 }
 
 // ---------------------------------------------------------------------------
@@ -538,18 +596,19 @@ __global__ void __launch_bounds__(kBlock) k_md_action(Geo g, OpK<double> k, cons
 }
 
 void norm2(cudaStream_t s, const Geo& g, const double2* v, double* dst, int accumulate, const Red& red) {
-  k_norm2<<<grid_of(g), kBlock, 0, s>>>(g.V, v, dst, accumulate, red);
+  k_norm2<<<occ_grid(k_norm2, nblocks(g.V)), kBlock, 0, s>>>(g.V, v, dst, accumulate, red);
 }
 void redot(cudaStream_t s, const Geo& g, const double2* u, const double2* v, double* dst, int accumulate,
            const Red& red) {
-  k_redot<<<grid_of(g), kBlock, 0, s>>>(g.V, u, v, dst, accumulate, red);
+  k_redot<<<occ_grid(k_redot, nblocks(g.V)), kBlock, 0, s>>>(g.V, u, v, dst, accumulate, red);
 }
 void gauge_action(cudaStream_t s, const Geo& g, const double2* A, double fac, double* dst, const Red& red) {
-  k_gauge_action<<<grid_of(g), kBlock, 0, s>>>(g.V, A, fac, dst, red);
+  k_gauge_action<<<occ_grid(k_gauge_action, nblocks(g.V)), kBlock, 0, s>>>(g.V, A, fac, dst, red);
 }
 void md_action(cudaStream_t s, const Geo& g, const OpK<double>& kd, const double2* nz, const double2* Wt,
                const double2* Wx, double* dst, const Red& red) {
-  TG_OP_DISPATCH(kd, (k_md_action<MU0><<<sgrid(g), kBlock, 0, s>>>(g, kd, nz, Wt, Wx, dst, red)));
+  TG_OP_DISPATCH(kd, (k_md_action<MU0><<<occ_grid(k_md_action<MU0>, stencil_work(g)), kBlock, 0, s>>>(
+                          g, kd, nz, Wt, Wx, dst, red)));
 }
 
 // ---------------------------------------------------------------------------

@@ -14,11 +14,11 @@ struct TrajStats {
   unsigned long long traj;   // Philox trajectory counter
 };
 
-struct CgBufs64 {          // FP64 CG work vectors
-  double2 *r, *p, *Mp;
+struct CgBufs64 {          // FP64 CG work vectors (p alternates between two buffers)
+  double2 *r, *p[2], *Mp;
 };
 struct CgBufsMixed {       // FP32 CG work vectors + FP64 accumulators
-  float2 *xs, *rs, *ps, *Mps;
+  float2 *xs, *rs, *ps[2], *Mps;
   double2* tmp64;          // M x for the reliable update
 };
 
@@ -47,14 +47,15 @@ void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, int dag, const 
 // CG on M^dag M (FP64).  km = M constants, kd = M^dag constants.
 void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
                CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int log_index, Cond c);
+// one iteration reading p[half] and writing p[half ^ 1]; iterations alternate half = 0, 1
 void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
-               double2* x, const CgBufs64& w, CgState* st, CgLog* log, const Red& red, Cond c);
+               double2* x, const CgBufs64& w, int half, CgState* st, CgLog* log, const Red& red, Cond c);
 // Mixed precision: FP32 iterations + FP64 reliable update
 void cgmx_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufsMixed& w, CgState* st,
                CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int ru_interval,
                int log_index, Cond c);
 void cgmx_iter(cudaStream_t s, const Geo& g, const OpK<float>& km, const OpK<float>& kd, const Links& L,
-               const CgBufsMixed& w, CgState* st, const Red& red, Cond c);
+               const CgBufsMixed& w, int half, CgState* st, const Red& red, Cond c);
 void cgmx_reliable(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
                    const double2* b, double2* x, const CgBufsMixed& w, CgState* st, CgLog* log, const Red& red,
                    Cond c);
