@@ -72,6 +72,8 @@ struct Geo {
 // the warp's edge).  Per site that leaves 3 coalesced loads (psi(t+1), Wt,
 // Wx) instead of 9.
 constexpr int kMarchT = 4;
+// Minimum resident blocks per SM the stencil kernels are compiled for.
+constexpr int kStencilBlocksPerSM = 1;  // no register cap: capping at 42 spilled heavily
 
 __device__ __forceinline__ void site_tx(const Geo& g, int s, int& t, int& x) {
   // V < 2^24 keeps float(s) exact; the fix-up absorbs the rounding of s/nx.

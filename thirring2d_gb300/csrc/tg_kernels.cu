@@ -147,6 +147,9 @@ __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld
   const int x = (xw << 5) + lane;
   const int xr = (x + 1 == nx) ? 0 : x + 1;
   const int xl = (x == 0) ? nx - 1 : x - 1;
+  // the one operand each lane fetches across the warp edge: lane 31 its right
+  // neighbour, lane 0 its left one, the others a duplicate (uniform, no branch)
+  const int xe = (lane == 31) ? xr : xl;
   const int tm = (t0 == 0) ? g.nt - 1 : t0 - 1;
   C2<R> pm = ld(tm * nx + x);
   C2<R> wtm = Wt[tm * nx + x];
@@ -159,13 +162,15 @@ __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld
     const C2<R> pp = ld(tp * nx + x);
     const C2<R> wt = Wt[s];
     const C2<R> wx = Wx[s];
+    const C2<R> pe = ld(t * nx + xe);
+    const C2<R> we = Wx[t * nx + xl];
     C2<R> pr = shfl_down1<R>(pc);
     C2<R> pl = shfl_up1<R>(pc);
     C2<R> wl = shfl_up1<R>(wx);
-    if (lane == 31) pr = ld(t * nx + xr);
+    if (lane == 31) pr = pe;
     if (lane == 0) {
-      pl = ld(t * nx + xl);
-      wl = Wx[t * nx + xl];
+      pl = pe;
+      wl = we;
     }
     epi(s, dslash_vals<R, DAG, MU0>(k, pc, pp, pm, pr, pl, wt, wtm, wx, wl), pc);
     pm = pc;
@@ -235,7 +240,7 @@ template <class K> int occ_grid(K kernel, int work) {
 }
 
 template <typename R, int DAG, bool MU0>
-__global__ void __launch_bounds__(kBlock) k_dslash(Geo g, OpK<R> k, const C2<R>* __restrict__ in,
+__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_dslash(Geo g, OpK<R> k, const C2<R>* __restrict__ in,
                                                    C2<R>* __restrict__ out, const C2<R>* __restrict__ Wt,
                                                    const C2<R>* __restrict__ Wx) {
   auto epi = [&](int s, C2<R> o, C2<R>) { out[s] = o; };
@@ -345,7 +350,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(Geo g, const double2* __rest
 }
 
 template <typename R, bool MU0>
-__global__ void __launch_bounds__(kBlock) k_cg1(Geo g, OpK<R> k, const C2<R>* __restrict__ r,
+__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cg1(Geo g, OpK<R> k, const C2<R>* __restrict__ r,
                                                 const C2<R>* __restrict__ p_old, C2<R>* __restrict__ p_new,
                                                 C2<R>* __restrict__ Mp, const C2<R>* __restrict__ Wt,
                                                 const C2<R>* __restrict__ Wx, CgState* st, Red red) {
@@ -373,7 +378,7 @@ __global__ void __launch_bounds__(kBlock) k_cg1(Geo g, OpK<R> k, const C2<R>* __
 
 // FP64: convergence tested on the recursive residual, as hmc.c:381.
 template <bool MU0>
-__global__ void __launch_bounds__(kBlock) k_cg2_64(Geo g, OpK<double> k, const double2* __restrict__ Mp,
+__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cg2_64(Geo g, OpK<double> k, const double2* __restrict__ Mp,
                                                    const double2* __restrict__ p, double2* __restrict__ x,
                                                    double2* __restrict__ r, const double2* __restrict__ Wt,
                                                    const double2* __restrict__ Wx, CgState* st, CgLog* log,
@@ -431,7 +436,7 @@ void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<do
 // the last one, when the FP32 residual reaches the target, and at the cap.
 // ---------------------------------------------------------------------------
 template <bool MU0>
-__global__ void __launch_bounds__(kBlock) k_cgmx2(Geo g, OpK<float> k, const float2* __restrict__ Mp,
+__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cgmx2(Geo g, OpK<float> k, const float2* __restrict__ Mp,
                                                   const float2* __restrict__ p, float2* __restrict__ xs,
                                                   float2* __restrict__ r, const float2* __restrict__ Wt,
                                                   const float2* __restrict__ Wx, CgState* st, Red red, Cond c) {
@@ -479,7 +484,7 @@ __global__ void __launch_bounds__(kBlock) k_ru1(int n, double2* x, float2* xs, c
 
 // reliable update 2: tmp = M x (FP64)
 template <bool MU0>
-__global__ void __launch_bounds__(kBlock) k_ru2(Geo g, OpK<double> k, const double2* __restrict__ x,
+__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_ru2(Geo g, OpK<double> k, const double2* __restrict__ x,
                                                 double2* __restrict__ tmp, const double2* __restrict__ Wt,
                                                 const double2* __restrict__ Wx, const CgState* st) {
   if (!st->need_ru || st->done) return;
@@ -489,7 +494,7 @@ __global__ void __launch_bounds__(kBlock) k_ru2(Geo g, OpK<double> k, const doub
 
 // reliable update 3: r = b - M^dag tmp (FP64), rs = (float) r, decide
 template <bool MU0>
-__global__ void __launch_bounds__(kBlock) k_ru3(Geo g, OpK<double> k, const double2* __restrict__ b,
+__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_ru3(Geo g, OpK<double> k, const double2* __restrict__ b,
                                                 const double2* __restrict__ tmp, float2* __restrict__ rs,
                                                 const double2* __restrict__ Wt, const double2* __restrict__ Wx,
                                                 CgState* st, CgLog* log, Red red, Cond c) {
@@ -585,7 +590,7 @@ __global__ void __launch_bounds__(kBlock) k_gauge_action(int n, const double2* _
 }
 
 template <bool MU0>
-__global__ void __launch_bounds__(kBlock) k_md_action(Geo g, OpK<double> k, const double2* __restrict__ nz,
+__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_md_action(Geo g, OpK<double> k, const double2* __restrict__ nz,
                                                       const double2* __restrict__ Wt, const double2* __restrict__ Wx,
                                                       double* dst, Red red) {
   double a = 0;
