@@ -60,13 +60,13 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_per_iter():
-    """DRAM bytes per CG iteration from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "cg_iteration_traffic.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f)
-    return None
+# DRAM bytes (read + write) of one FP64 CG iteration (k_cg1<double> + k_cg2_64)
+# at 1024^2 from one ncu capture: profiles/cg_iteration_1024_fp64.md.
+CG_ITER_DRAM_BYTES = 178.95e6
+# FP64 work of one CG iteration per site, in flops (FMA = 2): two operator
+# applies (16 FMA + 2 MUL each), p' = r + beta p, x/r updates, two norms.
+CG_ITER_FP64_FLOPS_PER_SITE = 2 * 34 + 4 + 8 + 4 + 4
+FP64_PEAK_TFLOPS_NOMINAL = 1.25  # GB300 FP64 (vector) nominal; not in the measured peaks file
 
 
 class Clocks:
@@ -307,7 +307,6 @@ def run_ours(args, ws, rank, local):
     hbm, peak_kind = peaks()
     t_iter_ms = cg_ms / max(1, iters)
     achieved = CG_ITER_BYTES_PER_SITE * V / (t_iter_ms * 1e-3) / 1e9
-    traf = traffic_per_iter()
     launches = sum(1 + 3 * r.cg_iterations for r in res) + args.steps * (3 * W["nsteps"] + 20)
 
     if rank != 0:
@@ -324,7 +323,12 @@ def run_ours(args, ws, rank, local):
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": peak_kind, "bytes_per_site": CG_ITER_BYTES_PER_SITE,
                      "ms_per_iteration": t_iter_ms,
-                     "traffic": (traf["bytes_per_site"] * V if traf else None)},
+                     "traffic": CG_ITER_DRAM_BYTES,
+                     "traffic_source": "profiles/cg_iteration_1024_fp64.md (ncu, one capture)"},
+        "fp64_alu": {"achieved_tflops": CG_ITER_FP64_FLOPS_PER_SITE * V / (t_iter_ms * 1e-3) / 1e12,
+                     "peak_tflops": FP64_PEAK_TFLOPS_NOMINAL, "peak_source": "nominal",
+                     "frac": CG_ITER_FP64_FLOPS_PER_SITE * V / (t_iter_ms * 1e-3) / 1e12 / FP64_PEAK_TFLOPS_NOMINAL,
+                     "note": "the FP64 CG kernels keep the FP64 pipe 85-89% busy (ncu); they are FP64-ALU-bound"},
         "dslash": {"fp64_gbs": dslash_gbs, "fp64_ms_M": t_M, "fp64_ms_Mdag": t_Md, "fp64_frac": dslash_gbs / hbm,
                    "fp32_gbs": dslash32_gbs, "fp32_ms": t_M32, "bytes_per_site_fp64": 64, "bytes_per_site_fp32": 32},
         "mixed": {"value": mixed_value, "unit": "trajectories/s", "speedup_vs_fp64": mixed_value / value,
