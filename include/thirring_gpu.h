@@ -181,6 +181,46 @@ int tg_trajectory(tg_lattice* L, const tg_hmc_params* p, tg_traj_result* r);
 int tg_trajectory_ext(tg_lattice* L, const tg_hmc_params* p, const double* eta, const double* mom,
                       const double* noise, double u_accept, tg_traj_result* r);
 
+/* ---- batched chains ------------------------------------------------------
+ * Many independent HMC chains (different NT x NX, m, g, mu, seed) advanced
+ * by one persistent kernel launch per trajectory: each thread block runs whole
+ * chain trajectories (hmc.c:671-746) taken from a work queue, largest first.
+ * The reference runs one chain per process; a batch replaces N such runs.
+ * Random fields are the Philox streams of TG_RNG_PHILOX keyed by each chain's
+ * seed, so chain k reproduces a tg_lattice trajectory with the same seed. */
+typedef struct tg_batch tg_batch;
+
+typedef struct {
+  int nt, nx;               /* lattice of this chain                           */
+  double m, g, mu;          /* its couplings                                   */
+  int bc_t, bc_x;           /* TG_BC_*                                         */
+  unsigned long long seed;  /* Philox key of this chain                        */
+} tg_chain_params;
+
+typedef struct {
+  int nsteps;               /* leapfrog steps per trajectory                   */
+  double tau;               /* trajectory length                               */
+  int stochastic_term;      /* as tg_hmc_params                                */
+  int use_graph;            /* launch through a cached CUDA graph              */
+  int block;                /* threads per block (128..512, multiple of 32); 0 = tuned default */
+  tg_cg_params cg;          /* per-chain solver                                */
+} tg_batch_params;
+
+/* A starts at 0 for every chain. */
+int tg_batch_create(const tg_chain_params* chains, int nchains, int device, tg_batch** out);
+int tg_batch_destroy(tg_batch* B);
+int tg_batch_size(const tg_batch* B, int* nchains, long long* total_sites);
+/* gauge field of one chain: double[nt*nx*2] */
+int tg_batch_set_gauge(tg_batch* B, int chain, const double* A);
+int tg_batch_get_gauge(tg_batch* B, int chain, double* A);
+/* One trajectory of every chain; results[nchains] (cg_ms = device time of the
+ * whole batch).  Returns the worst CG status over the chains. */
+int tg_batch_trajectory(tg_batch* B, const tg_batch_params* p, tg_traj_result* results);
+/* Times one trajectory at each candidate block size (128, 256, 384, 512) with
+ * the chains' state saved and restored around every trial, and makes the
+ * fastest the default (p->block = 0).  *best_ms = its device time. */
+int tg_batch_autotune(tg_batch* B, const tg_batch_params* p, int* best_block, double* best_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,101 @@
+"""Batched chains (tg_batch_*): every chain of a batch reproduces the
+single-lattice path with the same seed (same Philox fields, same arithmetic,
+different reduction order), mixed precision matches FP64 on dH and
+acceptance, and the autotuner leaves the chains' state untouched."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CHAINS = [
+    dict(nt=16, nx=16, m=0.5, g=0.5, mu=0.0, bc_t=-1, bc_x=1, seed=11),
+    dict(nt=24, nx=24, m=0.4, g=0.8, mu=0.0, bc_t=-1, bc_x=-1, seed=12),
+    dict(nt=32, nx=16, m=0.6, g=1.0, mu=0.2, bc_t=-1, bc_x=1, seed=13),
+    dict(nt=8, nx=40, m=0.45, g=0.3, mu=0.0, bc_t=-1, bc_x=1, seed=14),
+    dict(nt=48, nx=48, m=0.35, g=0.6, mu=0.0, bc_t=-1, bc_x=1, seed=15),
+]
+
+
+@pytest.fixture(scope="module")
+def tg():
+    import thirring2d_gb300 as tg
+    tg.native.load()
+    return tg
+
+
+def start_fields(chains):
+    rng = np.random.default_rng(7)
+    return [rng.normal(0, 0.2, (c["nt"], c["nx"], 2)) for c in chains]
+
+
+def make_batch(tg, chains, A0):
+    B = tg.Batch(chains)
+    for i, A in enumerate(A0):
+        B.set_gauge(i, A)
+    return B
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_matches_single_lattice(tg, precision):
+    A0 = start_fields(CHAINS)
+    cg = tg.cg_params(rel_tol=1e-12, abs_tol2=0.0, precision=precision, ru_interval=50)
+    B = make_batch(tg, CHAINS, A0)
+    bres = [B.trajectory(tg.batch_params(nsteps=20, cg=cg)) for _ in range(2)]
+    for i, c in enumerate(CHAINS):
+        L = tg.Lattice(c["nt"], c["nx"], c["m"], c["g"], c["mu"], c["bc_t"], c["bc_x"])
+        L.set_gauge(A0[i])
+        hp = tg.hmc_params(nsteps=20, rng=tg.native.RNG_PHILOX, seed=c["seed"], cg=cg)
+        for k in range(2):
+            r = L.update_gauge(hp)
+            b = bres[k][i]
+            assert b.status == 0 and r.status == 0
+            assert abs(b.Spf0 - r.Spf0) <= 1e-12 * abs(r.Spf0)       # same Philox fields
+            assert abs(b.dH - r.dH) <= 1e-8 * max(1.0, abs(r.dH)), (i, k, b.dH, r.dH)
+            assert b.accepted == r.accepted
+        assert np.abs(B.get_gauge(i) - L.get_gauge()).max() < 1e-9
+
+
+def test_batch_mixed_matches_fp64(tg):
+    A0 = start_fields(CHAINS)
+    out = []
+    for precision in (0, 1):
+        cg = tg.cg_params(rel_tol=1e-12, abs_tol2=0.0, precision=precision, ru_interval=50)
+        B = make_batch(tg, CHAINS, A0)
+        out.append(B.trajectory(tg.batch_params(nsteps=20, cg=cg)))
+    for a, b in zip(*out):
+        assert abs(a.dH - b.dH) <= 1e-8 * max(1.0, abs(a.dH))
+        assert a.accepted == b.accepted
+        assert b.reliable_updates >= 1
+
+
+def test_batch_autotune_keeps_state(tg):
+    A0 = start_fields(CHAINS)
+    bp = tg.batch_params(nsteps=10)
+    B1 = make_batch(tg, CHAINS, A0)
+    block, ms = B1.autotune(bp)
+    assert block in (128, 256, 384, 512) and ms > 0
+    B2 = make_batch(tg, CHAINS, A0)
+    r1 = B1.trajectory(tg.batch_params(nsteps=10, block=256))
+    r2 = B2.trajectory(tg.batch_params(nsteps=10, block=256))
+    assert [x.dH for x in r1] == [x.dH for x in r2]
+
+
+def test_batch_mixed_sizes_many_chains(tg):
+    """The C4 shape at reduced count: 64 chains, sides from {16..128}, each with
+    its own m, g and seed, graph-launched, three trajectories."""
+    rng = np.random.default_rng(4)
+    sides = [16, 24, 32, 48, 64, 96, 128]
+    chains = [dict(nt=int(L), nx=int(L), m=float(rng.uniform(0.05, 0.5)), g=float(rng.uniform(0.2, 1.2)), mu=0.0,
+                   bc_t=-1, bc_x=1, seed=int(1000 + k)) for k, L in enumerate(rng.choice(sides, 64))]
+    B = tg.Batch(chains)
+    for i, c in enumerate(chains):
+        B.set_gauge(i, rng.normal(0, 0.2, (c["nt"], c["nx"], 2)))
+    bp = tg.batch_params(nsteps=10, cg=tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=1))
+    prev = None
+    for _ in range(3):
+        res = B.trajectory(bp)
+        assert all(r.status == 0 and np.isfinite(r.dH) for r in res)
+        assert all(r.cg_solves == 11 for r in res)
+        if prev is not None:
+            assert any(a.Spf0 != b.Spf0 for a, b in zip(prev, res))   # fresh fields each trajectory
+        prev = res

@@ -1,0 +1,50 @@
+// tg_batch.h -- structures and launch interface of the batched-chain kernel
+// (tg_batch.cu), shared with the C ABI in tg_capi.cu.
+#pragma once
+
+#include "tg_internal.cuh"
+
+namespace tg {
+
+// One chain: geometry, couplings, seed, and where its sites start in the
+// packed field arrays (chains are concatenated site-major).
+struct BatchChain {
+  Geo geo;
+  double m, g, mu;
+  int bc_t, bc_x;
+  unsigned long long seed;
+  long long off;
+};
+
+// Packed per-site fields of all chains.
+struct BatchFields {
+  double2 *A, *An, *mom, *phi, *noise, *x, *Mx, *tmp, *Wt, *Wx, *r64, *p64, *Mp64;
+  float2 *Wt32, *Wx32, *xs, *rs, *ps, *Mps;
+};
+
+struct BatchCg {
+  double rel_tol, abs_tol2;
+  int maxiter, precision, ru_interval;
+};
+
+struct BatchTraj {
+  int nsteps;
+  double tau;
+  int stochastic_term;
+  BatchCg cg;
+};
+
+// Per-chain outcome of a trajectory; `traj` is the chain's Philox trajectory
+// counter (read at the start, incremented at the end).
+struct ChainResult {
+  double dH, Sg0, Spf0, Smd0, Smom0, Sg1, Spf1, Smd1, Smom1, u;
+  int accepted, status, cg_iterations, cg_max_iterations, reliable_updates, solves;
+  unsigned long long traj;
+};
+
+void batch_trajectory(cudaStream_t s, int grid, int block, const BatchChain* chains, const int* order, int n,
+                      const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue);
+// resident blocks per SM of the batch kernel at this block size (0 if it cannot launch)
+int batch_blocks_per_sm(int block);
+
+}  // namespace tg

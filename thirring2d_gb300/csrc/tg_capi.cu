@@ -7,10 +7,13 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <map>
+#include <numeric>
 #include <string>
 #include <vector>
 
+#include "tg_batch.h"
 #include "tg_launch.h"
 
 using namespace tg;
@@ -903,6 +906,285 @@ int tg_trajectory_ext(tg_lattice* L, const tg_hmc_params* p, const double* eta, 
   tg_hmc_params q = *p;
   q.rng = TG_RNG_EXTERNAL;
   return run_trajectory(L, q, r);
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched chains
+// ===========================================================================
+struct tg_batch {
+  int device = 0;
+  int n = 0;
+  long long total = 0;
+  std::vector<tg_chain_params> P;
+  std::vector<long long> off;
+  cudaStream_t stream = nullptr;
+  BatchChain* d_chains = nullptr;
+  int* d_order = nullptr;
+  ChainResult* d_res = nullptr;
+  ChainResult* h_res = nullptr;
+  unsigned* d_queue = nullptr;
+  BatchFields F{};
+  int sms = 1;
+  int tuned_block = 256;
+  std::map<std::string, GraphEntry> graphs;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+namespace {
+
+int batch_block(const tg_batch* B, const tg_batch_params& p) {
+  int b = p.block > 0 ? p.block : B->tuned_block;
+  return b;
+}
+
+int batch_launch(tg_batch* B, const tg_batch_params& p, int block, cudaStream_t s) {
+  if (block < 32 || block > 512 || block % 32) return fail(TG_E_ARG, "block must be a multiple of 32 in [32, 512]");
+  int per_sm = batch_blocks_per_sm(block);
+  if (per_sm <= 0) return fail(TG_E_CUDA, "batch kernel cannot launch at this block size");
+  int grid = std::min(B->n, per_sm * B->sms);
+  BatchTraj t;
+  t.nsteps = p.nsteps;
+  t.tau = p.tau;
+  t.stochastic_term = p.stochastic_term;
+  t.cg = BatchCg{p.cg.rel_tol, p.cg.abs_tol2, p.cg.maxiter, p.cg.precision, p.cg.ru_interval};
+  TG_CK(cudaMemsetAsync(B->d_queue, 0, sizeof(unsigned), s));
+  batch_trajectory(s, grid, block, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
+  TG_CK(cudaGetLastError());
+  return TG_OK;
+}
+
+int batch_run(tg_batch* B, const tg_batch_params& p, int block, double* ms) {
+  char buf[256];
+  snprintf(buf, sizeof buf, "b%d/%d/%.17g/%d/", block, p.nsteps, p.tau, p.stochastic_term);
+  std::string key = buf + cg_key(p.cg);
+  TG_CK(cudaEventRecord(B->e0, B->stream));
+  if (p.use_graph && env_graph_enabled()) {
+    auto it = B->graphs.find(key);
+    if (it == B->graphs.end()) {
+      GraphEntry ge;
+      TG_CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = batch_launch(B, p, block, B->stream);
+      cudaGraph_t gr = nullptr;
+      cudaError_t e = cudaStreamEndCapture(B->stream, &gr);
+      if (rc != TG_OK) {
+        if (gr) cudaGraphDestroy(gr);
+        return rc;
+      }
+      if (e != cudaSuccess) return fail(TG_E_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+      ge.graph = gr;
+      TG_CK(cudaGraphInstantiate(&ge.exec, gr, 0));
+      it = B->graphs.emplace(key, ge).first;
+    }
+    TG_CK(cudaGraphLaunch(it->second.exec, B->stream));
+  } else {
+    TG_TRY(batch_launch(B, p, block, B->stream));
+  }
+  TG_CK(cudaEventRecord(B->e1, B->stream));
+  TG_CK(cudaMemcpyAsync(B->h_res, B->d_res, sizeof(ChainResult) * B->n, cudaMemcpyDeviceToHost, B->stream));
+  TG_CK(cudaStreamSynchronize(B->stream));
+  float f = 0;
+  TG_CK(cudaEventElapsedTime(&f, B->e0, B->e1));
+  if (ms) *ms = f;
+  return TG_OK;
+}
+
+int check_batch_params(const tg_batch_params* p) {
+  if (!p) return fail(TG_E_ARG, "null batch parameters");
+  if (p->nsteps <= 0 || !(p->tau > 0)) return fail(TG_E_ARG, "nsteps and tau must be positive");
+  if (p->block < 0 || p->block > 512 || p->block % 32) return fail(TG_E_ARG, "block must be 0 or a multiple of 32 up to 512");
+  return check_cg_params(&p->cg);
+}
+
+}  // namespace
+
+extern "C" {
+
+int tg_batch_create(const tg_chain_params* chains, int nchains, int device, tg_batch** out) {
+  if (!chains || nchains <= 0 || !out) return fail(TG_E_ARG, "bad argument");
+  *out = nullptr;
+  TG_CK(cudaSetDevice(device));
+  tg_batch* B = new tg_batch();
+  auto bail = [&](int rc) { tg_batch_destroy(B); return rc; };
+  B->device = device;
+  B->n = nchains;
+  B->P.assign(chains, chains + nchains);
+  std::vector<BatchChain> hc(nchains);
+  long long total = 0;
+  for (int i = 0; i < nchains; i++) {
+    const tg_chain_params& c = chains[i];
+    auto bc_ok = [](int b) { return b == 1 || b == -1 || b == 0; };
+    if (c.nt < 2 || c.nx < 2 || (long long)c.nt * c.nx >= (1LL << 24) || !bc_ok(c.bc_t) || !bc_ok(c.bc_x) ||
+        !(c.g > 0))
+      return bail(fail(TG_E_ARG, "invalid chain " + std::to_string(i)));
+    BatchChain& b = hc[i];
+    memset(&b, 0, sizeof b);
+    b.geo.nt = c.nt;
+    b.geo.nx = c.nx;
+    b.geo.V = c.nt * c.nx;
+    b.geo.inv_nx = 1.0f / (float)c.nx;
+    b.m = c.m;
+    b.g = c.g;
+    b.mu = c.mu;
+    b.bc_t = c.bc_t;
+    b.bc_x = c.bc_x;
+    b.seed = c.seed;
+    b.off = total;
+    B->off.push_back(total);
+    total += b.geo.V;
+  }
+  B->total = total;
+  // largest estimated cost first: sites x 1/m (CG iterations grow like 1/m)
+  std::vector<int> order(nchains);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    double ca = (double)hc[a].geo.V / std::max(fabs(hc[a].m), 1e-3);
+    double cb = (double)hc[b].geo.V / std::max(fabs(hc[b].m), 1e-3);
+    return ca > cb;
+  });
+  if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&B->e0) != cudaSuccess || cudaEventCreate(&B->e1) != cudaSuccess)
+    return bail(fail(TG_E_CUDA, "stream/event creation failed"));
+  cudaDeviceGetAttribute(&B->sms, cudaDevAttrMultiProcessorCount, device);
+  if (B->sms <= 0) B->sms = 1;
+  int rc;
+  double2** d2[] = {&B->F.A, &B->F.An, &B->F.mom, &B->F.phi, &B->F.noise, &B->F.x, &B->F.Mx, &B->F.tmp,
+                    &B->F.Wt, &B->F.Wx, &B->F.r64, &B->F.p64, &B->F.Mp64};
+  for (auto pp : d2)
+    if ((rc = dmalloc(pp, (size_t)total)) != TG_OK) return bail(rc);
+  float2** f2[] = {&B->F.Wt32, &B->F.Wx32, &B->F.xs, &B->F.rs, &B->F.ps, &B->F.Mps};
+  for (auto pp : f2)
+    if ((rc = dmalloc(pp, (size_t)total)) != TG_OK) return bail(rc);
+  if ((rc = dmalloc(&B->d_chains, nchains)) != TG_OK || (rc = dmalloc(&B->d_order, nchains)) != TG_OK ||
+      (rc = dmalloc(&B->d_res, nchains)) != TG_OK || (rc = dmalloc(&B->d_queue, 1)) != TG_OK)
+    return bail(rc);
+  if (cudaMallocHost((void**)&B->h_res, sizeof(ChainResult) * nchains) != cudaSuccess)
+    return bail(fail(TG_E_ALLOC, "pinned allocation failed"));
+  if (cudaMemcpyAsync(B->d_chains, hc.data(), sizeof(BatchChain) * nchains, cudaMemcpyHostToDevice, B->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(B->d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, B->stream) !=
+          cudaSuccess ||
+      cudaMemsetAsync(B->d_res, 0, sizeof(ChainResult) * nchains, B->stream) != cudaSuccess ||
+      cudaMemsetAsync(B->F.A, 0, sizeof(double2) * total, B->stream) != cudaSuccess ||
+      cudaMemsetAsync(B->F.noise, 0, sizeof(double2) * total, B->stream) != cudaSuccess ||
+      cudaStreamSynchronize(B->stream) != cudaSuccess)
+    return bail(fail(TG_E_CUDA, "batch initialisation failed"));
+  *out = B;
+  return TG_OK;
+}
+
+int tg_batch_destroy(tg_batch* B) {
+  if (!B) return TG_OK;
+  cudaSetDevice(B->device);
+  if (B->stream) cudaStreamSynchronize(B->stream);
+  for (auto& kv : B->graphs) {
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  void* dev[] = {B->F.A, B->F.An, B->F.mom, B->F.phi, B->F.noise, B->F.x, B->F.Mx, B->F.tmp, B->F.Wt, B->F.Wx,
+                 B->F.r64, B->F.p64, B->F.Mp64, B->F.Wt32, B->F.Wx32, B->F.xs, B->F.rs, B->F.ps, B->F.Mps,
+                 B->d_chains, B->d_order, B->d_res, B->d_queue};
+  for (void* d : dev)
+    if (d) cudaFree(d);
+  if (B->h_res) cudaFreeHost(B->h_res);
+  if (B->e0) cudaEventDestroy(B->e0);
+  if (B->e1) cudaEventDestroy(B->e1);
+  if (B->stream) cudaStreamDestroy(B->stream);
+  delete B;
+  return TG_OK;
+}
+
+int tg_batch_size(const tg_batch* B, int* nchains, long long* total_sites) {
+  if (!B) return fail(TG_E_ARG, "null batch");
+  if (nchains) *nchains = B->n;
+  if (total_sites) *total_sites = B->total;
+  return TG_OK;
+}
+
+int tg_batch_set_gauge(tg_batch* B, int chain, const double* A) {
+  if (!B || !A || chain < 0 || chain >= B->n) return fail(TG_E_ARG, "bad argument");
+  size_t V = (size_t)B->P[chain].nt * B->P[chain].nx;
+  TG_CK(cudaMemcpyAsync(B->F.A + B->off[chain], A, V * sizeof(double2), cudaMemcpyHostToDevice, B->stream));
+  TG_CK(cudaStreamSynchronize(B->stream));
+  return TG_OK;
+}
+
+int tg_batch_get_gauge(tg_batch* B, int chain, double* A) {
+  if (!B || !A || chain < 0 || chain >= B->n) return fail(TG_E_ARG, "bad argument");
+  size_t V = (size_t)B->P[chain].nt * B->P[chain].nx;
+  TG_CK(cudaMemcpyAsync(A, B->F.A + B->off[chain], V * sizeof(double2), cudaMemcpyDeviceToHost, B->stream));
+  TG_CK(cudaStreamSynchronize(B->stream));
+  return TG_OK;
+}
+
+int tg_batch_trajectory(tg_batch* B, const tg_batch_params* p, tg_traj_result* results) {
+  if (!B) return fail(TG_E_ARG, "null batch");
+  TG_TRY(check_batch_params(p));
+  TG_CK(cudaSetDevice(B->device));
+  double ms = 0;
+  TG_TRY(batch_run(B, *p, batch_block(B, *p), &ms));
+  int worst = TG_OK;
+  for (int i = 0; i < B->n; i++) {
+    const ChainResult& c = B->h_res[i];
+    worst = std::max(worst, c.status);
+    if (!results) continue;
+    tg_traj_result& r = results[i];
+    memset(&r, 0, sizeof r);
+    r.dH = c.dH;
+    r.Sg0 = c.Sg0; r.Spf0 = c.Spf0; r.Smd0 = c.Smd0; r.Smom0 = c.Smom0;
+    r.Sg1 = c.Sg1; r.Spf1 = c.Spf1; r.Smd1 = c.Smd1; r.Smom1 = c.Smom1;
+    r.u_accept = c.u;
+    r.accepted = c.accepted;
+    r.status = c.status;
+    r.cg_solves = c.solves;
+    r.cg_iterations = c.cg_iterations;
+    r.cg_max_iterations = c.cg_max_iterations;
+    r.reliable_updates = c.reliable_updates;
+    r.cg_ms = ms;
+  }
+  return solver_status(worst);
+}
+
+int tg_batch_autotune(tg_batch* B, const tg_batch_params* p, int* best_block, double* best_ms) {
+  if (!B) return fail(TG_E_ARG, "null batch");
+  TG_TRY(check_batch_params(p));
+  TG_CK(cudaSetDevice(B->device));
+  // save the chains' state (gauge fields and trajectory counters)
+  double2* A0 = nullptr;
+  ChainResult* R0 = nullptr;
+  TG_TRY(dmalloc(&A0, (size_t)B->total));
+  if (dmalloc(&R0, (size_t)B->n) != TG_OK) { cudaFree(A0); return TG_E_ALLOC; }
+  auto cleanup = [&]() { cudaFree(A0); cudaFree(R0); };
+  if (cudaMemcpyAsync(A0, B->F.A, sizeof(double2) * B->total, cudaMemcpyDeviceToDevice, B->stream) != cudaSuccess ||
+      cudaMemcpyAsync(R0, B->d_res, sizeof(ChainResult) * B->n, cudaMemcpyDeviceToDevice, B->stream) != cudaSuccess) {
+    cleanup();
+    return fail(TG_E_CUDA, "autotune state copy failed");
+  }
+  const int cand[] = {128, 256, 384, 512};
+  int best = 0;
+  double bms = 1e300;
+  for (int b : cand) {
+    if (batch_blocks_per_sm(b) <= 0) continue;
+    double ms = 0;
+    tg_batch_params q = *p;
+    q.use_graph = 0;
+    int rc = batch_run(B, q, b, &ms);
+    if (rc == TG_OK && ms < bms) { bms = ms; best = b; }
+    if (cudaMemcpyAsync(B->F.A, A0, sizeof(double2) * B->total, cudaMemcpyDeviceToDevice, B->stream) != cudaSuccess ||
+        cudaMemcpyAsync(B->d_res, R0, sizeof(ChainResult) * B->n, cudaMemcpyDeviceToDevice, B->stream) !=
+            cudaSuccess) {
+      cleanup();
+      return fail(TG_E_CUDA, "autotune state restore failed");
+    }
+  }
+  cudaStreamSynchronize(B->stream);
+  cleanup();
+  if (!best) return fail(TG_E_CUDA, "no block size could run the batch kernel");
+  B->tuned_block = best;
+  if (best_block) *best_block = best;
+  if (best_ms) *best_ms = bms;
+  return TG_OK;
 }
 
 }  // extern "C"

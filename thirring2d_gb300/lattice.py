@@ -183,3 +183,62 @@ class Lattice:
         N.check(self.lib.tg_trajectory_ext(self.h, C.byref(hp), _p(eta), _p(mom), _p(nz) if nz is not None else None,
                                            u_accept, C.byref(r)), True)
         return r
+
+
+def batch_params(nsteps=10, tau=1.0, stochastic_term=True, use_graph=True, block=0, cg=None) -> N.BatchParams:
+    """Settings of a batched trajectory (block = 0: the tuned default)."""
+    return N.BatchParams(nsteps, tau, int(stochastic_term), int(use_graph), block, cg or cg_params(rel_tol=1e-10,
+                                                                                                  abs_tol2=0.0))
+
+
+class Batch:
+    """Many independent chains advanced together (tg_batch_*).  `chains` is a
+    list of dicts with keys nt, nx, m, g, mu, bc_t, bc_x, seed."""
+
+    def __init__(self, chains, device: int = 0):
+        self.lib = N.load()
+        self.shapes = [(c["nt"], c["nx"]) for c in chains]
+        arr = (N.ChainParams * len(chains))(*[
+            N.ChainParams(c["nt"], c["nx"], c["m"], c.get("g", 0.5), c.get("mu", 0.0), c.get("bc_t", -1),
+                          c.get("bc_x", -1), c.get("seed", 0)) for c in chains])
+        h = C.c_void_p()
+        N.check(self.lib.tg_batch_create(arr, len(chains), device, C.byref(h)))
+        self.h = h
+        self.n = len(chains)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def total_sites(self) -> int:
+        n, t = C.c_int(), C.c_longlong()
+        N.check(self.lib.tg_batch_size(self.h, C.byref(n), C.byref(t)))
+        return t.value
+
+    def set_gauge(self, i: int, A):
+        nt, nx = self.shapes[i]
+        A = _f64(A).reshape(nt, nx, 2)
+        N.check(self.lib.tg_batch_set_gauge(self.h, i, _p(A)))
+
+    def get_gauge(self, i: int) -> np.ndarray:
+        nt, nx = self.shapes[i]
+        A = np.empty((nt, nx, 2))
+        N.check(self.lib.tg_batch_get_gauge(self.h, i, _p(A)))
+        return A
+
+    def trajectory(self, bp: N.BatchParams | None = None):
+        res = (N.TrajResult * self.n)()
+        N.check(self.lib.tg_batch_trajectory(self.h, C.byref(bp or batch_params()), res), True)
+        return list(res)
+
+    def autotune(self, bp: N.BatchParams | None = None):
+        b, ms = C.c_int(), C.c_double()
+        N.check(self.lib.tg_batch_autotune(self.h, C.byref(bp or batch_params()), C.byref(b), C.byref(ms)))
+        return b.value, ms.value

@@ -49,6 +49,16 @@ class TrajResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ChainParams(C.Structure):
+    _fields_ = [("nt", C.c_int), ("nx", C.c_int), ("m", C.c_double), ("g", C.c_double), ("mu", C.c_double),
+                ("bc_t", C.c_int), ("bc_x", C.c_int), ("seed", C.c_ulonglong)]
+
+
+class BatchParams(C.Structure):
+    _fields_ = [("nsteps", C.c_int), ("tau", C.c_double), ("stochastic_term", C.c_int), ("use_graph", C.c_int),
+                ("block", C.c_int), ("cg", CgParams)]
+
+
 class TGError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"thirring_gpu error {STATUS_NAMES.get(code, code)}: {msg}")
@@ -89,6 +99,13 @@ SIGNATURES = {
     "tg_puregauge_ext": (C.c_int, [_vp, _dp, C.c_int]),
     "tg_trajectory": (C.c_int, [_vp, C.POINTER(HmcParams), C.POINTER(TrajResult)]),
     "tg_trajectory_ext": (C.c_int, [_vp, C.POINTER(HmcParams), _dp, _dp, _dp, C.c_double, C.POINTER(TrajResult)]),
+    "tg_batch_create": (C.c_int, [C.POINTER(ChainParams), C.c_int, C.c_int, C.POINTER(_vp)]),
+    "tg_batch_destroy": (C.c_int, [_vp]),
+    "tg_batch_size": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
+    "tg_batch_set_gauge": (C.c_int, [_vp, C.c_int, _dp]),
+    "tg_batch_get_gauge": (C.c_int, [_vp, C.c_int, _dp]),
+    "tg_batch_trajectory": (C.c_int, [_vp, C.POINTER(BatchParams), C.POINTER(TrajResult)]),
+    "tg_batch_autotune": (C.c_int, [_vp, C.POINTER(BatchParams), C.POINTER(C.c_int), _dp]),
 }
 
 _lib = None

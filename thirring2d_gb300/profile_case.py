@@ -27,7 +27,12 @@ def main():
     ap.add_argument("--applies", type=int, default=20)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--graph", type=int, default=1)
+    ap.add_argument("--batch", type=int, default=0, help="run the batched-chain case with this many chains")
+    ap.add_argument("--trajectories", type=int, default=2)
+    ap.add_argument("--sequential", type=int, default=0, help="chains to also run one at a time (FP64 path)")
     a = ap.parse_args()
+    if a.batch:
+        return batch_case(a)
     n = a.size
     rng = np.random.default_rng(n)
     L = Lattice(n, n, 0.05, 0.6, 0.0, N.BC_ANTIPERIODIC, N.BC_PERIODIC)
@@ -46,6 +51,54 @@ def main():
         out["cg_iterations"] = res.iterations
         out["cg_status"] = N.STATUS_NAMES[res.status]
     L.close()
+    print(json.dumps(out))
+
+
+def c4_chains(n: int, seed: int = 4):
+    """The batched-chain workload: n chains, sides uniform in {16, 24, 32, 48, 64,
+    96, 128}, m ~ U[0.05, 0.5], g ~ U[0.2, 1.2], own seeds, A ~ N(0, 0.2^2)."""
+    rng = np.random.default_rng(seed)
+    sides = np.array([16, 24, 32, 48, 64, 96, 128])
+    chains, fields = [], []
+    for k in range(n):
+        L = int(rng.choice(sides))
+        chains.append(dict(nt=L, nx=L, m=float(rng.uniform(0.05, 0.5)), g=float(rng.uniform(0.2, 1.2)), mu=0.0,
+                           bc_t=N.BC_ANTIPERIODIC, bc_x=N.BC_PERIODIC, seed=int(seed * 100000 + k)))
+        fields.append(rng.normal(0, 0.2, (L, L, 2)))
+    return chains, fields
+
+
+def batch_case(a):
+    import time
+
+    from .lattice import Batch, batch_params, hmc_params
+    chains, fields = c4_chains(a.batch)
+    B = Batch(chains)
+    for i, A in enumerate(fields):
+        B.set_gauge(i, A)
+    prec = N.PREC_MIXED if a.precision == "mixed" else N.PREC_FP64
+    bp = batch_params(nsteps=10, use_graph=bool(a.graph),
+                      cg=cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=prec, ru_interval=50))
+    block, tune_ms = B.autotune(bp)
+    out = {"chains": a.batch, "sites": B.total_sites(), "precision": a.precision, "block": block,
+           "tune_ms": tune_ms, "traj_ms": []}
+    for _ in range(a.trajectories):
+        res = B.trajectory(bp)
+        out["traj_ms"].append(res[0].cg_ms)
+        out["status"] = max(r.status for r in res)
+        out["acceptance"] = float(np.mean([r.accepted for r in res]))
+        out["cg_iterations_mean"] = float(np.mean([r.cg_iterations for r in res]))
+    B.close()
+    if a.sequential:
+        cg64 = cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=N.PREC_FP64)
+        t0 = time.perf_counter()
+        for c, A in list(zip(chains, fields))[: a.sequential]:
+            L = Lattice(c["nt"], c["nx"], c["m"], c["g"], c["mu"], c["bc_t"], c["bc_x"])
+            L.set_gauge(A)
+            L.update_gauge(hmc_params(nsteps=10, rng=N.RNG_PHILOX, seed=c["seed"], cg=cg64))
+            L.close()
+        out["sequential_fp64_s"] = time.perf_counter() - t0
+        out["sequential_chains"] = a.sequential
     print(json.dumps(out))
 
 
