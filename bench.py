@@ -304,6 +304,8 @@ def run_ours(args, ws, rank, local):
     ms_mx = allmax(ws, ms_mx)
     mixed_value = ws * args.steps / (ms_mx / 1000.0)
 
+    batched = run_batched(tg, torch, dev, args) if not args.no_batched else None
+
     hbm, peak_kind = peaks()
     t_iter_ms = cg_ms / max(1, iters)
     achieved = CG_ITER_BYTES_PER_SITE * V / (t_iter_ms * 1e-3) / 1e9
@@ -335,6 +337,7 @@ def run_ours(args, ws, rank, local):
                   "cg_iterations_per_traj": statistics.mean(r.cg_iterations for r in res_mx),
                   "reliable_updates_per_traj": statistics.mean(r.reliable_updates for r in res_mx),
                   "dH_pairs_fp64_vs_mixed": mx_pairs},
+        "batched": batched,
         "cg_iterations_per_traj": iters / args.steps,
         "dH": [r.dH for r in res], "accepted": [r.accepted for r in res],
         "clocks": clocks, "gpu_launches": launches,
@@ -345,12 +348,73 @@ def run_ours(args, ws, rank, local):
     print(json.dumps(line))
 
 
+def run_batched(tg, torch, dev, args, nchains=512, sample=32):
+    """The batched-chain workload (512 chains, sides in {16..128}, m ~ U[0.05, 0.5],
+    g ~ U[0.2, 1.2], 10 leapfrog steps, CG 1e-10): mixed-precision batch in one
+    launch per trajectory vs the same chains one at a time on the plain FP64
+    single-lattice path (a sample of `sample` chains, scaled)."""
+    from thirring2d_gb300.profile_case import c4_chains
+    chains, fields = c4_chains(nchains)
+    cgm = tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=tg.native.PREC_MIXED, ru_interval=50)
+    cg64 = tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=tg.native.PREC_FP64)
+
+    def make(cg):
+        B = tg.Batch(chains)
+        for i, A in enumerate(fields):
+            B.set_gauge(i, A)
+        return B, tg.batch_params(nsteps=10, cg=cg)
+
+    Bm, bpm = make(cgm)
+    cfg, _ = Bm.autotune(bpm)
+    B64, bp64 = make(cg64)
+    first_m, first_64 = Bm.trajectory(bpm), B64.trajectory(bp64)   # same fields, same Philox stream
+    dh_err = max(abs(a.dH - b.dH) / max(1.0, abs(b.dH)) for a, b in zip(first_m, first_64))
+    acc_mismatch = sum(a.accepted != b.accepted for a, b in zip(first_m, first_64))
+    B64.close()
+    steps = max(1, args.steps)
+    ms = 0.0
+    res = []
+    for _ in range(steps):
+        r = Bm.trajectory(bpm)
+        ms += r[0].cg_ms
+        res.append(r)
+    batched_rate = nchains * steps / (ms / 1e3)
+    # one at a time on the FP64 single-lattice path: one warm-up trajectory per
+    # chain (graph capture), then one timed with CUDA events on its stream
+    seq_ms = 0.0
+    for c, A in list(zip(chains, fields))[:sample]:
+        L = tg.Lattice(c["nt"], c["nx"], c["m"], c["g"], c["mu"], c["bc_t"], c["bc_x"])
+        L.set_gauge(A)
+        hp = tg.hmc_params(nsteps=10, rng=tg.native.RNG_PHILOX, seed=c["seed"], cg=cg64)
+        L.update_gauge(hp)
+        st = torch.cuda.ExternalStream(L.lib.tg_stream(L.h), device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        L.update_gauge(hp)
+        e1.record(st)
+        torch.cuda.synchronize()
+        seq_ms += e0.elapsed_time(e1)
+        L.close()
+    seq_rate = sample / (seq_ms / 1e3)
+    Bm.close()
+    return {"value": batched_rate, "unit": "chain-trajectories/s", "chains": nchains,
+            "sites": int(sum(c["nt"] * c["nx"] for c in chains)), "precision": "mixed (FP32 CG + FP64 reliable updates)",
+            "kernel_instance": cfg, "ms_per_batch_trajectory": ms / steps,
+            "sequential_fp64": {"value": seq_rate, "unit": "chain-trajectories/s",
+                                "sample": f"{sample} of the {nchains} chains, one at a time, second trajectory each"},
+            "speedup_vs_sequential_fp64": batched_rate / seq_rate,
+            "dH_rel_err_vs_fp64_batch_max": dh_err, "accept_mismatch_vs_fp64": acc_mismatch,
+            "acceptance": float(np.mean([r.accepted for r in res[-1]])),
+            "cg_iterations_per_chain_traj": float(np.mean([r.cg_iterations for r in res[-1]]))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-chain measurement")
     args = ap.parse_args()
     ws, rank, local = dist_init()
     if args.impl == "reference":

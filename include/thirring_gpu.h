@@ -202,7 +202,7 @@ typedef struct {
   double tau;               /* trajectory length                               */
   int stochastic_term;      /* as tg_hmc_params                                */
   int use_graph;            /* launch through a cached CUDA graph              */
-  int block;                /* threads per block (128..512, multiple of 32); 0 = tuned default */
+  int block;                /* threads per block: 128, 256, 384 or 512; 0 = the tuned kernel instance */
   tg_cg_params cg;          /* per-chain solver                                */
 } tg_batch_params;
 
@@ -216,9 +216,12 @@ int tg_batch_get_gauge(tg_batch* B, int chain, double* A);
 /* One trajectory of every chain; results[nchains] (cg_ms = device time of the
  * whole batch).  Returns the worst CG status over the chains. */
 int tg_batch_trajectory(tg_batch* B, const tg_batch_params* p, tg_traj_result* results);
-/* Times one trajectory at each candidate block size (128, 256, 384, 512) with
- * the chains' state saved and restored around every trial, and makes the
- * fastest the default (p->block = 0).  *best_ms = its device time. */
+/* Times one trajectory with every compiled instance of the batch kernel
+ * (threads per block x minimum resident blocks per SM, which trades registers
+ * against occupancy), with the chains' state saved and restored around every
+ * trial, and makes the fastest the default (p->block = 0).
+ * *best_block = 100 * threads + blocks per SM of the winner; *best_ms = its
+ * device time. */
 int tg_batch_autotune(tg_batch* B, const tg_batch_params* p, int* best_block, double* best_ms);
 
 #ifdef __cplusplus

@@ -25,8 +25,6 @@
 
 namespace tg {
 
-constexpr int kBatchMaxBlock = 512;
-
 // ---------------------------------------------------------------------------
 // Block-wide primitives (all threads of the block call them)
 // ---------------------------------------------------------------------------
@@ -237,7 +235,7 @@ __device__ __forceinline__ CgOut block_cg(const ChainCtx& c, const BatchCg& P, c
 // One trajectory of one chain (update_gauge, hmc.c:671-746), by one block.
 // ---------------------------------------------------------------------------
 template <bool MU0>
-__device__ void chain_trajectory(ChainCtx& c, const BatchTraj& P, ChainResult* res) {
+__device__ void chain_trajectory(const ChainCtx& c, const BatchTraj& P, ChainResult* res) {
   const int V = c.g.V;
   const Geo& g = c.g;
   OpK<double> km{c.m, c.ep, -c.em, MU0}, kd{c.m, -c.em, c.ep, MU0};
@@ -344,20 +342,31 @@ __device__ void chain_trajectory(ChainCtx& c, const BatchTraj& P, ChainResult* r
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kBatchMaxBlock) k_batch_trajectory(const BatchChain* __restrict__ chains,
-                                                                     const int* __restrict__ order, int n,
-                                                                     BatchFields F, BatchTraj P,
-                                                                     ChainResult* results, unsigned* queue) {
+__device__ __forceinline__ void fill_ctx(ChainCtx& c, const BatchChain& b, const BatchFields& F);
+
+template <int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_batch_trajectory(const BatchChain* __restrict__ chains,
+                                                               const int* __restrict__ order, int n,
+                                                               BatchFields F, BatchTraj P, ChainResult* results,
+                                                               unsigned* queue) {
+  // The chain context (geometry, couplings, ~20 field pointers) lives in shared
+  // memory: kept in registers it would cost ~40 of them per thread.
   __shared__ int next;
+  __shared__ ChainCtx c;
   while (true) {
     if (threadIdx.x == 0) next = (int)atomicAdd(queue, 1u);
     __syncthreads();
     const int q = next;
-    __syncthreads();
     if (q >= n) break;
     const int ci = order[q];
-    const BatchChain& b = chains[ci];
-    ChainCtx c;
+    if (threadIdx.x == 0) fill_ctx(c, chains[ci], F);
+    __syncthreads();
+    if (c.mu == 0.0) chain_trajectory<true>(c, P, &results[ci]);
+    else chain_trajectory<false>(c, P, &results[ci]);
+  }
+}
+
+__device__ __forceinline__ void fill_ctx(ChainCtx& c, const BatchChain& b, const BatchFields& F) {
     c.g = b.geo;
     c.m = b.m;
     c.gc = b.g;
@@ -373,19 +382,44 @@ __global__ void __launch_bounds__(kBatchMaxBlock) k_batch_trajectory(const Batch
     c.r64 = F.r64 + o; c.p64 = F.p64 + o; c.Mp64 = F.Mp64 + o;
     c.Wt32 = F.Wt32 + o; c.Wx32 = F.Wx32 + o; c.xs = F.xs + o; c.rs = F.rs + o; c.ps = F.ps + o;
     c.Mps = F.Mps + o;
-    if (b.mu == 0.0) chain_trajectory<true>(c, P, &results[ci]);
-    else chain_trajectory<false>(c, P, &results[ci]);
+}
+
+// The kernel instances the autotuner chooses from: (threads per block,
+// minimum resident blocks per SM).  More blocks per SM cap the registers (64 at
+// 2048 resident threads, with small spills in the reliable-update path);
+// fewer leave them uncapped (about 120).
+const BatchCfg kBatchCfgs[kBatchNumCfgs] = {{128, 8}, {256, 4}, {256, 2}, {384, 2}, {512, 2}, {512, 1}};
+
+template <int BS, int MINB> const void* batch_kernel() { return (const void*)k_batch_trajectory<BS, MINB>; }
+
+static const void* batch_kernel_of(int cfg) {
+  switch (cfg) {
+    case 0: return batch_kernel<128, 8>();
+    case 1: return batch_kernel<256, 4>();
+    case 2: return batch_kernel<256, 2>();
+    case 3: return batch_kernel<384, 2>();
+    case 4: return batch_kernel<512, 2>();
+    default: return batch_kernel<512, 1>();
   }
 }
 
-void batch_trajectory(cudaStream_t s, int grid, int block, const BatchChain* chains, const int* order, int n,
+void batch_trajectory(cudaStream_t s, int cfg, int grid, const BatchChain* chains, const int* order, int n,
                       const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue) {
-  k_batch_trajectory<<<grid, block, 0, s>>>(chains, order, n, F, P, results, queue);
+  switch (cfg) {
+    case 0: k_batch_trajectory<128, 8><<<grid, 128, 0, s>>>(chains, order, n, F, P, results, queue); break;
+    case 1: k_batch_trajectory<256, 4><<<grid, 256, 0, s>>>(chains, order, n, F, P, results, queue); break;
+    case 2: k_batch_trajectory<256, 2><<<grid, 256, 0, s>>>(chains, order, n, F, P, results, queue); break;
+    case 3: k_batch_trajectory<384, 2><<<grid, 384, 0, s>>>(chains, order, n, F, P, results, queue); break;
+    case 4: k_batch_trajectory<512, 2><<<grid, 512, 0, s>>>(chains, order, n, F, P, results, queue); break;
+    default: k_batch_trajectory<512, 1><<<grid, 512, 0, s>>>(chains, order, n, F, P, results, queue); break;
+  }
 }
 
-int batch_blocks_per_sm(int block) {
+int batch_blocks_per_sm(int cfg) {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_trajectory, block, 0) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_kernel_of(cfg), kBatchCfgs[cfg].block, 0) !=
+      cudaSuccess)
+    return 0;
   return nb;
 }
 

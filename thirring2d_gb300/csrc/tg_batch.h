@@ -42,9 +42,16 @@ struct ChainResult {
   unsigned long long traj;
 };
 
-void batch_trajectory(cudaStream_t s, int grid, int block, const BatchChain* chains, const int* order, int n,
+// kernel instances of the batched trajectory: threads per block, min blocks per SM
+struct BatchCfg {
+  int block, minb;
+};
+constexpr int kBatchNumCfgs = 6;
+extern const BatchCfg kBatchCfgs[kBatchNumCfgs];
+
+void batch_trajectory(cudaStream_t s, int cfg, int grid, const BatchChain* chains, const int* order, int n,
                       const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue);
-// resident blocks per SM of the batch kernel at this block size (0 if it cannot launch)
-int batch_blocks_per_sm(int block);
+// resident blocks per SM of kernel instance cfg (0 if it cannot launch)
+int batch_blocks_per_sm(int cfg);
 
 }  // namespace tg

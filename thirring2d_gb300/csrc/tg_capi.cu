@@ -927,21 +927,25 @@ struct tg_batch {
   unsigned* d_queue = nullptr;
   BatchFields F{};
   int sms = 1;
-  int tuned_block = 256;
+  int tuned_cfg = 1;  // index into kBatchCfgs
   std::map<std::string, GraphEntry> graphs;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
 };
 
 namespace {
 
-int batch_block(const tg_batch* B, const tg_batch_params& p) {
-  int b = p.block > 0 ? p.block : B->tuned_block;
-  return b;
+// kernel instance for p.block: the tuned one, else the instance with that
+// block size and the most resident blocks per SM
+int batch_cfg(const tg_batch* B, const tg_batch_params& p) {
+  if (p.block <= 0) return B->tuned_cfg;
+  for (int c = 0; c < kBatchNumCfgs; c++)
+    if (kBatchCfgs[c].block == p.block) return c;
+  return -1;
 }
 
-int batch_launch(tg_batch* B, const tg_batch_params& p, int block, cudaStream_t s) {
-  if (block < 32 || block > 512 || block % 32) return fail(TG_E_ARG, "block must be a multiple of 32 in [32, 512]");
-  int per_sm = batch_blocks_per_sm(block);
+int batch_launch(tg_batch* B, const tg_batch_params& p, int cfg, cudaStream_t s) {
+  if (cfg < 0 || cfg >= kBatchNumCfgs) return fail(TG_E_ARG, "block must be 0, 128, 256, 384 or 512");
+  int per_sm = batch_blocks_per_sm(cfg);
   if (per_sm <= 0) return fail(TG_E_CUDA, "batch kernel cannot launch at this block size");
   int grid = std::min(B->n, per_sm * B->sms);
   BatchTraj t;
@@ -950,14 +954,14 @@ int batch_launch(tg_batch* B, const tg_batch_params& p, int block, cudaStream_t 
   t.stochastic_term = p.stochastic_term;
   t.cg = BatchCg{p.cg.rel_tol, p.cg.abs_tol2, p.cg.maxiter, p.cg.precision, p.cg.ru_interval};
   TG_CK(cudaMemsetAsync(B->d_queue, 0, sizeof(unsigned), s));
-  batch_trajectory(s, grid, block, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
+  batch_trajectory(s, cfg, grid, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
   TG_CK(cudaGetLastError());
   return TG_OK;
 }
 
-int batch_run(tg_batch* B, const tg_batch_params& p, int block, double* ms) {
+int batch_run(tg_batch* B, const tg_batch_params& p, int cfg, double* ms) {
   char buf[256];
-  snprintf(buf, sizeof buf, "b%d/%d/%.17g/%d/", block, p.nsteps, p.tau, p.stochastic_term);
+  snprintf(buf, sizeof buf, "b%d/%d/%.17g/%d/", cfg, p.nsteps, p.tau, p.stochastic_term);
   std::string key = buf + cg_key(p.cg);
   TG_CK(cudaEventRecord(B->e0, B->stream));
   if (p.use_graph && env_graph_enabled()) {
@@ -965,7 +969,7 @@ int batch_run(tg_batch* B, const tg_batch_params& p, int block, double* ms) {
     if (it == B->graphs.end()) {
       GraphEntry ge;
       TG_CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
-      int rc = batch_launch(B, p, block, B->stream);
+      int rc = batch_launch(B, p, cfg, B->stream);
       cudaGraph_t gr = nullptr;
       cudaError_t e = cudaStreamEndCapture(B->stream, &gr);
       if (rc != TG_OK) {
@@ -979,7 +983,7 @@ int batch_run(tg_batch* B, const tg_batch_params& p, int block, double* ms) {
     }
     TG_CK(cudaGraphLaunch(it->second.exec, B->stream));
   } else {
-    TG_TRY(batch_launch(B, p, block, B->stream));
+    TG_TRY(batch_launch(B, p, cfg, B->stream));
   }
   TG_CK(cudaEventRecord(B->e1, B->stream));
   TG_CK(cudaMemcpyAsync(B->h_res, B->d_res, sizeof(ChainResult) * B->n, cudaMemcpyDeviceToHost, B->stream));
@@ -993,7 +997,8 @@ int batch_run(tg_batch* B, const tg_batch_params& p, int block, double* ms) {
 int check_batch_params(const tg_batch_params* p) {
   if (!p) return fail(TG_E_ARG, "null batch parameters");
   if (p->nsteps <= 0 || !(p->tau > 0)) return fail(TG_E_ARG, "nsteps and tau must be positive");
-  if (p->block < 0 || p->block > 512 || p->block % 32) return fail(TG_E_ARG, "block must be 0 or a multiple of 32 up to 512");
+  if (p->block != 0 && p->block != 128 && p->block != 256 && p->block != 384 && p->block != 512)
+    return fail(TG_E_ARG, "block must be 0, 128, 256, 384 or 512");
   return check_cg_params(&p->cg);
 }
 
@@ -1123,7 +1128,7 @@ int tg_batch_trajectory(tg_batch* B, const tg_batch_params* p, tg_traj_result* r
   TG_TRY(check_batch_params(p));
   TG_CK(cudaSetDevice(B->device));
   double ms = 0;
-  TG_TRY(batch_run(B, *p, batch_block(B, *p), &ms));
+  TG_TRY(batch_run(B, *p, batch_cfg(B, *p), &ms));
   int worst = TG_OK;
   for (int i = 0; i < B->n; i++) {
     const ChainResult& c = B->h_res[i];
@@ -1161,16 +1166,15 @@ int tg_batch_autotune(tg_batch* B, const tg_batch_params* p, int* best_block, do
     cleanup();
     return fail(TG_E_CUDA, "autotune state copy failed");
   }
-  const int cand[] = {128, 256, 384, 512};
-  int best = 0;
+  int best = -1;
   double bms = 1e300;
-  for (int b : cand) {
-    if (batch_blocks_per_sm(b) <= 0) continue;
+  for (int c = 0; c < kBatchNumCfgs; c++) {
+    if (batch_blocks_per_sm(c) <= 0) continue;
     double ms = 0;
     tg_batch_params q = *p;
     q.use_graph = 0;
-    int rc = batch_run(B, q, b, &ms);
-    if (rc == TG_OK && ms < bms) { bms = ms; best = b; }
+    int rc = batch_run(B, q, c, &ms);
+    if (rc == TG_OK && ms < bms) { bms = ms; best = c; }
     if (cudaMemcpyAsync(B->F.A, A0, sizeof(double2) * B->total, cudaMemcpyDeviceToDevice, B->stream) != cudaSuccess ||
         cudaMemcpyAsync(B->d_res, R0, sizeof(ChainResult) * B->n, cudaMemcpyDeviceToDevice, B->stream) !=
             cudaSuccess) {
@@ -1180,9 +1184,9 @@ int tg_batch_autotune(tg_batch* B, const tg_batch_params* p, int* best_block, do
   }
   cudaStreamSynchronize(B->stream);
   cleanup();
-  if (!best) return fail(TG_E_CUDA, "no block size could run the batch kernel");
-  B->tuned_block = best;
-  if (best_block) *best_block = best;
+  if (best < 0) return fail(TG_E_CUDA, "no kernel instance could run the batch");
+  B->tuned_cfg = best;
+  if (best_block) *best_block = kBatchCfgs[best].block * 100 + kBatchCfgs[best].minb;
   if (best_ms) *best_ms = bms;
   return TG_OK;
 }
