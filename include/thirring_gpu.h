@@ -151,6 +151,10 @@ int tg_md_action(tg_lattice* L, const double* n, double* S);
  * momentum_step (hmc.c:504-661) subtracts, from npf solved vectors
  * chi_k = (M^dag M)^-1 phi_k (double[npf*V*2]); noise may be NULL. */
 int tg_force(tg_lattice* L, int npf, const double* chi, const double* noise, double* F);
+/* dS_pf/dA alone -- the pseudofermion force of hmc.c:517-576, summed over
+ * npf pseudofermions phi (double[npf*V*2]) -- solving chi_k = (M^dag M)^-1
+ * phi_k afresh (the solution is not kept).  F: double[V*2]. */
+int tg_pf_force(tg_lattice* L, const tg_cg_params* cp, int npf, const double* phi, double* F, tg_cg_result* res);
 /* momentum_step (hmc.c:504-665): mom -= eps * dS/dA, solving for every
  * pseudofermion; res (may be NULL) receives the summed CG counts. */
 int tg_momentum_step(tg_lattice* L, const tg_cg_params* cp, double* mom, int npf, const double* phi,

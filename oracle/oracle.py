@@ -153,6 +153,16 @@ class Oracle:
                                _ptr(nz) if nz is not None else None, _ptr(F))
         return F
 
+    def pf_force(self, A, chis) -> np.ndarray:
+        """dS_pf/dA alone for solved chi_k (hmc.c:517-576)."""
+        A = _f64(A)
+        chis = _c128(np.asarray(chis).reshape(-1, self.nt, self.nx))
+        F = np.zeros((self.nt, self.nx, 2), np.float64)
+        for c in chis:
+            Mc = self.M(A, c)
+            self.L.orc_pf_force(C.byref(self.lat), _ptr(A), _ptr(_c128(c)), _ptr(Mc), _ptr(F))
+        return F
+
     def momentum_step(self, A, p, phis, noise, eps, rel_tol=0.0, abs_tol2=1e-30, maxiter=100000):
         A = _f64(A)
         p = _f64(p).copy()

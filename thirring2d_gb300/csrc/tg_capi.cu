@@ -779,6 +779,32 @@ int tg_force(tg_lattice* L, int npf, const double* chi, const double* noise, dou
   return download(L, F, L->vout, 2 * V);
 }
 
+int tg_pf_force(tg_lattice* L, const tg_cg_params* cp, int npf, const double* phi, double* F, tg_cg_result* res) {
+  if (!L || !F || npf <= 0 || npf > kMaxPf || !phi) return fail(TG_E_ARG, "bad argument");
+  TG_TRY(check_cg_params(cp));
+  const size_t V = (size_t)L->V;
+  TG_TRY(ensure_pf(L, npf));
+  const double ep = exp(L->P.mu), em = exp(-L->P.mu);
+  TG_TRY(upload(L, L->phi, phi, 2 * V * npf));
+  TG_CK(cudaMemsetAsync(L->vout, 0, V * sizeof(double2), L->stream));  // F accumulates in vout
+  tg_cg_result acc{};
+  for (int k = 0; k < npf; k++) {
+    tg_cg_result r{};
+    TG_TRY(solve_dev(L, *cp, L->phi + V * k, L->chi, &r));
+    acc.iterations += r.iterations;
+    acc.reliable_updates += r.reliable_updates;
+    if (r.status > acc.status) acc.status = r.status;
+    acc.rr = r.rr;
+    acc.rr0 = r.rr0;
+    dslash64(L->stream, L->g, op_k(L, 0), 0, L->chi, L->Mchi, L->Wt, L->Wx);
+    force_field(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, nullptr, L->vout, 0.0, 0);
+  }
+  TG_CK(cudaGetLastError());
+  if (res) *res = acc;
+  TG_TRY(download(L, F, L->vout, 2 * V));
+  return solver_status(acc.status);
+}
+
 int tg_momentum_step(tg_lattice* L, const tg_cg_params* cp, double* mom, int npf, const double* phi,
                      const double* noise, double eps, tg_cg_result* res) {
   if (!L || !mom || npf < 0 || npf > kMaxPf || (npf > 0 && !phi)) return fail(TG_E_ARG, "bad argument");

@@ -146,6 +146,15 @@ class Lattice:
         N.check(self.lib.tg_force(self.h, len(chis), _p(chis), _p(nz) if nz is not None else None, _p(F)))
         return F
 
+    def pf_force(self, phis, cp: N.CgParams | None = None):
+        """dS_pf/dA for pseudofermions phis ([npf, nt, nx]); solves afresh.  Returns (F, CgResult)."""
+        phis = _c128(np.asarray(phis).reshape(-1, self.nt, self.nx))
+        F = np.empty((self.nt, self.nx, 2))
+        res = N.CgResult()
+        N.check(self.lib.tg_pf_force(self.h, C.byref(cp or cg_params()), len(phis), _p(phis), _p(F), C.byref(res)),
+                True)
+        return F, res
+
     def momentum_step(self, mom, phis, noise, eps, cp: N.CgParams | None = None):
         mom = _f64(mom).copy()
         phis = _c128(np.asarray(phis).reshape(-1, self.nt, self.nx))

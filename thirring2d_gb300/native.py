@@ -93,6 +93,7 @@ SIGNATURES = {
     "tg_momentum_step": (C.c_int, [_vp, C.POINTER(CgParams), _dp, C.c_int, _dp, _dp, C.c_double,
                                    C.POINTER(CgResult)]),
     "tg_gauge_step": (C.c_int, [_vp, _dp, C.c_double]),
+    "tg_pf_force": (C.c_int, [_vp, C.POINTER(CgParams), C.c_int, _dp, _dp, C.POINTER(CgResult)]),
     "tg_mt_seed": (C.c_int, [_vp, C.c_long, C.c_long]),
     "tg_mt_uniforms": (C.c_int, [_vp, _dp, C.c_long]),
     "tg_puregauge_sweeps": (C.c_int, [_vp, C.c_int]),

@@ -30,9 +30,12 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="run the batched-chain case with this many chains")
     ap.add_argument("--trajectories", type=int, default=2)
     ap.add_argument("--sequential", type=int, default=0, help="chains to also run one at a time (FP64 path)")
+    ap.add_argument("--c5", action="store_true", help="the 64^2 differentiation / dH-scaling report")
     a = ap.parse_args()
     if a.batch:
         return batch_case(a)
+    if a.c5:
+        return c5_case(a)
     n = a.size
     rng = np.random.default_rng(n)
     L = Lattice(n, n, 0.05, 0.6, 0.0, N.BC_ANTIPERIODIC, N.BC_PERIODIC)
@@ -99,6 +102,41 @@ def batch_case(a):
             L.close()
         out["sequential_fp64_s"] = time.perf_counter() - t0
         out["sequential_chains"] = a.sequential
+    print(json.dumps(out))
+
+
+def c5_case(a):
+    """64^2, m 0.1, g 0.5, A ~ N(0, 0.3^2), two pseudofermions: dH statistics over
+    a.trajectories trajectories at leapfrog step sizes 0.2, 0.1, 0.05 (and 0.025,
+    0.0125 over fewer), FP64 and mixed precision on the same Philox stream."""
+    from .lattice import hmc_params
+    n = 64
+    A0 = np.random.default_rng(64).normal(0, 0.3, (n, n, 2))
+    out = {"lattice": f"{n}x{n}", "m": 0.1, "g": 0.5, "npf": 2, "rows": []}
+    for nsteps, ntraj in ((5, a.trajectories), (10, a.trajectories), (20, a.trajectories),
+                          (40, max(1, a.trajectories // 5)), (80, max(1, a.trajectories // 5))):
+        row = {"eps": 1.0 / nsteps, "trajectories": ntraj}
+        dhs = {}
+        for prec, name in ((N.PREC_FP64, "fp64"), (N.PREC_MIXED, "mixed")):
+            L = Lattice(n, n, 0.1, 0.5, 0.0, N.BC_ANTIPERIODIC, N.BC_PERIODIC)
+            L.set_gauge(A0)
+            hp = hmc_params(nsteps=nsteps, tau=1.0, npf=2, stochastic_term=False, rng=N.RNG_PHILOX, seed=55,
+                            cg=cg_params(rel_tol=1e-12, abs_tol2=0.0, precision=prec, ru_interval=50))
+            res = [L.update_gauge(hp) for _ in range(ntraj)]
+            L.close()
+            dh = np.array([r.dH for r in res])
+            dhs[name] = (dh, [r.accepted for r in res])
+            row[name] = {"mean_dH": float(dh.mean()), "mean_abs_dH": float(np.abs(dh).mean()),
+                         "rms_dH": float(np.sqrt((dh ** 2).mean())), "median_abs_dH": float(np.median(np.abs(dh))),
+                         "acceptance": float(np.mean([r.accepted for r in res])),
+                         "mean_exp_minus_dH": float(np.mean(np.exp(-np.clip(dh, -50, 50)))),
+                         "status": max(r.status for r in res)}
+        d64, dmx = dhs["fp64"][0], dhs["mixed"][0]
+        row["max_abs_dH_diff_mixed_vs_fp64"] = float(np.abs(d64 - dmx).max())
+        row["max_rel_dH_diff_mixed_vs_fp64"] = float((np.abs(d64 - dmx) / np.maximum(1.0, np.abs(d64))).max())
+        row["accept_mismatch"] = int(sum(x != y for x, y in zip(dhs["fp64"][1], dhs["mixed"][1])))
+        out["rows"].append(row)
+        print(json.dumps(row), flush=True)
     print(json.dumps(out))
 
 
