@@ -185,6 +185,24 @@ int tg_trajectory(tg_lattice* L, const tg_hmc_params* p, tg_traj_result* r);
 int tg_trajectory_ext(tg_lattice* L, const tg_hmc_params* p, const double* eta, const double* mom,
                       const double* noise, double u_accept, tg_traj_result* r);
 
+/* ---- CG without allocation -------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * programs whose device memory is fully budgeted up front (a framework's
+ * caching allocator owns the free memory) or that must not stall other
+ * streams (cudaMalloc/cudaFree can synchronize the device).  Solves
+ * M^dagger M x = b like tg_cg (FP64 solver only) on the calling thread's
+ * current device, with no tg_lattice and no allocation of any kind: every
+ * work vector lives in one fixed device array inside the library, sized for
+ * lattices of at most 16384 sites (128 x 128); larger lattices get TG_E_ARG.
+ * A_dev: gauge field double[nt*nx*2]; b_dev, x_dev: double2[nt*nx] on that
+ * device; p->device is not used; stream may be NULL (the default stream).
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the array and it
+ * keeps the previous call's contents, so calls that overlap on the GPU race:
+ * order them (one stream, or synchronize between them). */
+int tg_cg_noalloc(const tg_lattice_params* p, const tg_cg_params* cp, const void* A_dev, const void* b_dev,
+                  void* x_dev, tg_cg_result* res, void* stream);
+
 /* ---- batched chains ------------------------------------------------------
  * Many independent HMC chains (different NT x NX, m, g, mu, seed) advanced
  * by one persistent kernel launch per trajectory: each thread block runs whole

@@ -513,6 +513,11 @@ int run_trajectory(tg_lattice* L, const tg_hmc_params& p, tg_traj_result* r) {
 
 }  // namespace
 
+namespace tg {
+// error recording for entry points defined in other translation units
+int record_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace tg
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

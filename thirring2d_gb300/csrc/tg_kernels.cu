@@ -658,3 +658,45 @@ void accept_copy(cudaStream_t s, const Geo& g, const TrajStats* ts, double2* A, 
 }
 
 }  // namespace tg
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// Launchers with an explicit grid, for callers that must not touch the
+// occupancy cache above (it grows a host-side map): the allocation-free CG
+// entry point (tg_noalloc.cu).  Same kernels, same arithmetic.
+// ---------------------------------------------------------------------------
+int resident_grid_nocache(const void* kernel, int work) {
+  int dev = 0, sms = 1, per_sm = 1;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm <= 0)
+    per_sm = 1;
+  const int grid = per_sm * sms;
+  return grid < work ? grid : (work > 0 ? work : 1);
+}
+
+void link_phase_fixed(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,
+                      float2* Wt32, float2* Wx32) {
+  k_link_phase<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, Wt, Wx, Wt32, Wx32);
+}
+
+void cg64_init_fixed(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
+                     const Red& red, double rel_tol, double abs_tol2, int maxiter) {
+  const int grid = resident_grid_nocache((const void*)k_cg_init<double>, nblocks(g.V));
+  k_cg_init<double><<<grid, kBlock, 0, s>>>(g, b, x, w.r, w.p[0], nullptr, rel_tol, abs_tol2, maxiter, 0, -1, st,
+                                            nullptr, red, Cond{0, 0, 0});
+}
+
+void cg64_iter_fixed(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
+                     double2* x, const CgBufs64& w, int half, CgState* st, const Red& red) {
+  const int wk = stencil_work(g);
+  const double2* p_old = w.p[half];
+  double2* p_new = w.p[half ^ 1];
+  TG_OP_DISPATCH(km, (k_cg1<double, MU0><<<resident_grid_nocache((const void*)k_cg1<double, MU0>, wk), kBlock, 0,
+                                          s>>>(g, km, w.r, p_old, p_new, w.Mp, L.Wt, L.Wx, st, red)));
+  TG_OP_DISPATCH(kd, (k_cg2_64<MU0><<<resident_grid_nocache((const void*)k_cg2_64<MU0>, wk), kBlock, 0, s>>>(
+                          g, kd, w.Mp, p_new, x, w.r, L.Wt, L.Wx, st, nullptr, red, Cond{0, 0, 0})));
+}
+
+}  // namespace tg

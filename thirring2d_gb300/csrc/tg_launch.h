@@ -87,4 +87,13 @@ void accept_copy(cudaStream_t s, const Geo& g, const TrajStats* ts, double2* A, 
 // one pure-gauge Metropolis sweep over the 2V links; u[4V]; c = -Nf/g
 void puregauge(cudaStream_t s, const Geo& g, double* A, const double* u, double c);
 
+// Explicit-grid launchers used by the allocation-free CG entry point.
+int resident_grid_nocache(const void* kernel, int work);
+void link_phase_fixed(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,
+                      float2* Wt32, float2* Wx32);
+void cg64_init_fixed(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
+                     const Red& red, double rel_tol, double abs_tol2, int maxiter);
+void cg64_iter_fixed(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
+                     double2* x, const CgBufs64& w, int half, CgState* st, const Red& red);
+
 }  // namespace tg
