@@ -185,6 +185,32 @@ int tg_trajectory(tg_lattice* L, const tg_hmc_params* p, tg_traj_result* r);
 int tg_trajectory_ext(tg_lattice* L, const tg_hmc_params* p, const double* eta, const double* mom,
                       const double* noise, double u_accept, tg_traj_result* r);
 
+/* ---- measurements -------------------------------------------------------- */
+/* magnetisation of measure() (hmc.c:831-839): sum of A over sites and
+ * directions divided by NT*NX. */
+int tg_magnetisation(tg_lattice* L, double* M);
+/* fermion_phase (hmc.c:794-815): (1/sources) sum_k Im <c_k, M^dag c_k> over
+ * Gaussian sources.  noise: double[sources*V*2], or NULL to draw V pairs per
+ * source from the lattice's reference MT stream in hmc.c's order. */
+int tg_fermion_phase(tg_lattice* L, int sources, const double* noise, double* phase);
+/* Stochastic chiral condensate (no counterpart in hmc.c):
+ * pbp = (1/2V) mean_k Re <eta_k, M^-1 eta_k> over `sources` complex Gaussian
+ * Philox sources (E[eta eta^dag] = 2), M^-1 = (M^dag M)^-1 M^dag by CG;
+ * *err = standard error over the sources (may be NULL). */
+int tg_chiral_condensate(tg_lattice* L, const tg_cg_params* cp, int sources, unsigned long long seed, double* pbp,
+                         double* err);
+
+/* ---- fermion-bag operator (vec_ops.c) ------------------------------------ */
+/* fM / fM_transpose (vec_ops.c:96-174): the real, gauge-field-free staggered
+ * operator with occupied sites (mask[s] != 0) acting as the identity and
+ * skipped as neighbours; uses the lattice's m, mu and boundary conditions
+ * (the reference's ANTISYMMETRIC build: both antiperiodic).  Host double[V]. */
+int tg_fm_apply(tg_lattice* L, const int* mask, const double* in, double* out, int transpose);
+/* cg_MdM (vec_ops.c:261-307): CG on fM^T fM from x = 0; the reference stops
+ * at |r|^2 < 1e-30 (Thirring.h:42) within 10000 iterations (Thirring.h:43). */
+int tg_cg_mdm_masked(tg_lattice* L, const tg_cg_params* cp, const int* mask, const double* b, double* x,
+                     tg_cg_result* res);
+
 /* ---- CG without allocation -------------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:
  * programs whose device memory is fully budgeted up front (a framework's

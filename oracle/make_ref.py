@@ -131,6 +131,45 @@ def generate() -> str:
     return os.path.join(SRC, "hmc_patched.c")
 
 
+VSRC = os.path.join(SRC, "vecops")
+VEC_SIZES = [(8, 8), (6, 4), (16, 16)]
+
+
+def generate_vecops() -> None:
+    """The fermion-bag operator: vec_ops.c unchanged, next to a copy of
+    Thirring.h whose ``#define NT 64`` / ``#define NX 64`` become REF_NT / REF_NX
+    (vec_ops.c includes "Thirring.h" from its own directory, so both sit in
+    oracle/_ref/src/vecops/)."""
+    os.makedirs(VSRC, exist_ok=True)
+    with open(os.path.join(REF_ROOT, "Thirring.h")) as f:
+        text = f.read()
+    text = _sub(r"^#define NT 64\s*$", "#define NT REF_NT", text, 1, re.M)
+    text = _sub(r"^#define NX 64\s*$", "#define NX REF_NX", text, 1, re.M)
+    with open(os.path.join(VSRC, "Thirring.h"), "w") as f:
+        f.write("/* GENERATED by oracle/make_ref.py from rantahar/Thirring2D Thirring.h -- do not commit. */\n" + text)
+    for name in ("vec_ops.c", "mersenne_inline.c", "mersenne.h"):
+        with open(os.path.join(REF_ROOT, name)) as fi, open(os.path.join(VSRC, name), "w") as fo:
+            fo.write(fi.read())
+    with open(os.path.join(VSRC, "lapacke.h"), "w") as f:
+        f.write("void LAPACK_zgetrf(int* m, int* n, _Complex double* a, int* lda, int* ipiv, int* info);\n")
+
+
+def vec_lib_path(nt: int, nx: int) -> str:
+    return os.path.join(OUT, f"libvecopsref_T{nt}X{nx}.so")
+
+
+def build_vec_one(nt: int, nx: int) -> str:
+    out = vec_lib_path(nt, nx)
+    driver = os.path.join(HERE, "vecops_driver.c")
+    srcs = [driver, os.path.join(VSRC, "vec_ops.c"), os.path.join(VSRC, "mersenne_inline.c")]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(s) for s in srcs):
+        return out
+    cmd = (["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", "-w", "-Wl,-Bsymbolic", f"-I{VSRC}",
+            f"-DREF_NT={nt}", f"-DREF_NX={nx}", "-o", out] + srcs + ["-lm"])
+    subprocess.run(cmd, check=True)
+    return out
+
+
 def lib_path(nt: int, nx: int, variant: str) -> str:
     return os.path.join(OUT, f"libhmcref_T{nt}X{nx}_{variant}.so")
 
@@ -160,6 +199,7 @@ def build(sizes=None, variants=None) -> list[str]:
     """Generate (if the reference tree is present) and compile the oracle/_ref libraries."""
     if os.path.exists(os.path.join(REF_ROOT, "hmc.c")):
         generate()
+        generate_vecops()
     elif not os.path.exists(os.path.join(SRC, "hmc_patched.c")):
         return []
     sizes = sizes or DEFAULT_SIZES
@@ -167,7 +207,10 @@ def build(sizes=None, variants=None) -> list[str]:
     jobs = [(nt, nx, v) for (nt, nx) in sizes for v in variants]
     jobs += [(nt, nx, "sample_px") for (nt, nx) in SAMPLE_SIZES if (nt, nx) in sizes]
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
-        return list(ex.map(lambda j: build_one(*j), jobs))
+        libs = list(ex.map(lambda j: build_one(*j), jobs))
+        if os.path.exists(os.path.join(VSRC, "vec_ops.c")):
+            libs += list(ex.map(lambda j: build_vec_one(*j), VEC_SIZES))
+    return libs
 
 
 if __name__ == "__main__":

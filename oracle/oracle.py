@@ -302,3 +302,41 @@ def _ref_dense(self):
 
 
 RefHMC.dense_M = _ref_dense
+
+
+def vec_ref_lib_path(nt: int, nx: int) -> str:
+    return os.path.join(REF_DIR, f"libvecopsref_T{nt}X{nx}.so")
+
+
+class RefVecOps:
+    """A private instance of the reference's vec_ops.c (fM, fM_transpose,
+    cg_MdM of the fermion-bag programs; ANTISYMMETRIC build)."""
+
+    def __init__(self, nt, nx, m, mu=0.0):
+        src = vec_ref_lib_path(nt, nx)
+        if not os.path.exists(src):
+            raise FileNotFoundError(f"{src} not built (python oracle/make_ref.py)")
+        self._tmp = tempfile.mkdtemp(prefix="vecref_")
+        path = os.path.join(self._tmp, os.path.basename(src))
+        shutil.copy(src, path)
+        self.L = C.CDLL(path)
+        self.nt, self.nx = nt, nx
+        self.L.vref_setup(C.c_double(m), C.c_double(mu))
+
+    def __del__(self):
+        shutil.rmtree(getattr(self, "_tmp", ""), ignore_errors=True)
+
+    def set_field(self, mask):
+        self.L.vref_set_field(_ptr(np.ascontiguousarray(mask, dtype=np.int32), _ip))
+
+    def fM(self, v, transpose=False):
+        v = _f64(v)
+        out = np.empty_like(v)
+        self.L.vref_fM(_ptr(v), _ptr(out), int(transpose))
+        return out
+
+    def cg_MdM(self, b):
+        b = _f64(b)
+        x = np.empty_like(b)
+        self.L.vref_cg_MdM(_ptr(b), _ptr(x))
+        return x

@@ -104,8 +104,31 @@ def make_dense():
         np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **d)
 
 
+VEC_CONFIGS = {  # name: (nt, nx, m, mu, fraction of occupied sites, seed)
+    "vecops_8x8": (8, 8, 0.3, 0.2, 0.3, 1),
+    "vecops_6x4": (6, 4, 0.5, 0.0, 0.25, 2),
+    "vecops_16x16": (16, 16, 0.1, 0.0, 0.1, 3),
+}
+
+
+def make_vecops():
+    """fM, fM_transpose and cg_MdM of the reference's vec_ops.c (fermion-bag
+    operator, ANTISYMMETRIC boundaries) on random occupations."""
+    from oracle.oracle import RefVecOps
+    for name, (nt, nx, m, mu, occ, seed) in VEC_CONFIGS.items():
+        rng = np.random.default_rng(seed)
+        mask = (rng.random((nt, nx)) < occ).astype(np.int32)
+        v = rng.normal(size=(nt, nx))
+        b = rng.normal(size=(nt, nx))
+        ref = RefVecOps(nt, nx, m, mu)
+        ref.set_field(mask)
+        np.savez_compressed(os.path.join(OUT, f"{name}.npz"), nt=nt, nx=nx, m=m, mu=mu, mask=mask, v=v, b=b,
+                            fM_v=ref.fM(v), fMt_v=ref.fM(v, True), cg_x=ref.cg_MdM(b))
+
+
 if __name__ == "__main__":
     make_ref.build([(c[0], c[1]) for c in CONFIGS.values()] + [(4, 4), (6, 4)])
+    make_vecops()
     make_mt()
     make_dense()
     for name, cfg in CONFIGS.items():

@@ -1,0 +1,71 @@
+"""Beside the HMC path: the fermion-bag operator of vec_ops.c and its CG
+(against the reference's own outputs), and the measurements of hmc.c's
+measure() plus a stochastic chiral condensate (against the oracle / exact
+inverse)."""
+import numpy as np
+import pytest
+
+from helpers import golden, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def tg():
+    import thirring2d_gb300 as tg
+    tg.native.load()
+    return tg
+
+
+@pytest.mark.parametrize("name", ["vecops_8x8", "vecops_6x4", "vecops_16x16"])
+def test_masked_operator_golden(tg, name):
+    d = golden(name)
+    L = tg.Lattice(int(d["nt"]), int(d["nx"]), float(d["m"]), 0.5, float(d["mu"]), -1, -1)
+    assert np.abs(L.fM(d["mask"], d["v"]) - d["fM_v"]).max() < 1e-14
+    assert np.abs(L.fM(d["mask"], d["v"], True) - d["fMt_v"]).max() < 1e-14
+    x, res = L.cg_MdM(d["mask"], d["b"], tg.cg_params(maxiter=10000))   # vec_ops.c's stop, |r|^2 < 1e-30
+    assert res.status == 0
+    assert rel(x, d["cg_x"]) < 1e-12
+
+
+def test_masked_operator_all_occupied_is_identity(tg):
+    L = tg.Lattice(8, 8, 0.3, 0.5, 0.0, -1, -1)
+    v = np.random.default_rng(1).normal(size=(8, 8))
+    assert np.array_equal(L.fM(np.ones((8, 8), np.int32), v), v)
+
+
+def test_magnetisation(tg):
+    A = np.random.default_rng(2).normal(0, 0.7, (12, 20, 2))
+    L = tg.Lattice(12, 20, 0.2)
+    L.set_gauge(A)
+    assert abs(L.magnetisation() - A.sum() / (12 * 20)) < 1e-13
+
+
+def test_fermion_phase_reference_stream(tg, oracle_lib):
+    """fermion_phase (hmc.c:794-815) with sources from the reference MT stream."""
+    nt, nx, mu = 8, 8, 0.4
+    A = np.random.default_rng(3).normal(0, 0.5, (nt, nx, 2))
+    L = tg.Lattice(nt, nx, 0.3, 0.5, mu, -1, -1)
+    L.set_gauge(A)
+    L.seed_mersenne(99, 1000)
+    got = L.fermion_phase(20)
+    o = oracle_lib.Oracle(nt, nx, 0.3, 0.5, mu, -1, -1)
+    mt = oracle_lib.MT(99, 1000)
+    im = 0.0
+    for _ in range(20):
+        c, _ = mt.gaussian_field(nt, nx)
+        mdc = o.Mdag(A, c)
+        im += float((c.real * mdc.imag - c.imag * mdc.real).sum())
+    assert abs(got - im / 20) < 1e-11 * max(1.0, abs(im / 20))
+    assert abs(got) > 1e-6   # nonzero at mu != 0
+
+
+def test_chiral_condensate_against_exact_trace(tg, oracle_lib):
+    nt, nx, m = 8, 8, 0.3
+    A = np.random.default_rng(4).normal(0, 0.5, (nt, nx, 2))
+    L = tg.Lattice(nt, nx, m, 0.5, 0.0, -1, 1)
+    L.set_gauge(A)
+    pbp, err = L.chiral_condensate(400, seed=5, cp=tg.cg_params(rel_tol=1e-12, abs_tol2=0.0))
+    o = oracle_lib.Oracle(nt, nx, m, 0.5, 0.0, -1, 1)
+    exact = float(np.trace(np.linalg.inv(o.dense_M(A))).real) / (nt * nx)
+    assert err > 0 and abs(pbp - exact) < 5 * err, (pbp, exact, err)

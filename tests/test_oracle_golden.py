@@ -112,3 +112,14 @@ def test_force_finite_difference(oracle_lib):
         Am[t, xx, dr] -= h
         fd = (S(Ap) - S(Am)) / (2 * h)
         assert abs(fd - F[t, xx, dr]) < 1e-6 * max(1.0, abs(fd))
+
+
+@pytest.mark.parametrize("name", ["vecops_8x8", "vecops_6x4", "vecops_16x16"])
+def test_masked_operator_oracle(oracle_lib, name):
+    """The fermion-bag operator of vec_ops.c:96-174 and its CG (261-307)."""
+    d = golden(name)
+    o = oracle_lib.Oracle(int(d["nt"]), int(d["nx"]), float(d["m"]), 0.5, float(d["mu"]), -1, -1)
+    assert np.abs(o.fM(d["mask"], d["v"]) - d["fM_v"]).max() < 1e-14
+    assert np.abs(o.fM(d["mask"], d["v"], True) - d["fMt_v"]).max() < 1e-14
+    x, st, it = o.cg_MdM(d["mask"], d["b"], maxiter=10000)
+    assert st == 0 and rel(x, d["cg_x"]) < 1e-12

@@ -110,6 +110,8 @@ struct tg_lattice {
   double2 *mom = nullptr, *noise = nullptr, *chi = nullptr, *Mchi = nullptr, *vin = nullptr, *vout = nullptr;
   double2 *eta = nullptr, *phi = nullptr;  // [npf_alloc][V]
   double* unif = nullptr;                  // [4V] uniforms of one pure-gauge sweep (allocated on first use)
+  int* mask = nullptr;                     // masked real operator: occupation mask and 6 real vectors
+  double* rv[6] = {};                      // in/b, out/x, r, p, tmp, Ap (allocated on first use)
   int npf_alloc = 0;
   CgBufs64 w64{};
   CgBufsMixed wmx{};
@@ -606,7 +608,8 @@ int tg_destroy(tg_lattice* L) {
   void* dev[] = {L->A, L->Anew, L->Wt, L->Wx, L->mom, L->noise, L->chi, L->Mchi, L->vin, L->vout, L->w64.r,
                  L->w64.p[0], L->w64.p[1], L->w64.Mp, L->wmx.tmp64, L->Wt32, L->Wx32, L->wmx.xs, L->wmx.rs,
                  L->wmx.ps[0], L->wmx.ps[1], L->wmx.Mps,
-                 L->st, L->log, L->ts, L->red.partials, L->red.counter, L->eta, L->phi, L->unif};
+                 L->st, L->log, L->ts, L->red.partials, L->red.counter, L->eta, L->phi, L->unif, L->mask,
+                 L->rv[0], L->rv[1], L->rv[2], L->rv[3], L->rv[4], L->rv[5]};
   for (void* d : dev)
     if (d) cudaFree(d);
   void* hst[] = {L->h_stage, L->h_st, L->h_ts, L->h_log};
@@ -892,6 +895,130 @@ int tg_puregauge_sweeps(tg_lattice* L, int sweeps) {
     TG_TRY(tg_puregauge_ext(L, u.data(), 1));
   }
   return TG_OK;
+}
+
+// ---- measurements (hmc.c:794-842) and the masked real operator (vec_ops.c) ----
+namespace {
+int ensure_real(tg_lattice* L) {
+  if (L->mask) return TG_OK;
+  TG_TRY(dmalloc(&L->mask, (size_t)L->V));
+  for (int k = 0; k < 6; k++) TG_TRY(dmalloc(&L->rv[k], (size_t)L->V));
+  return TG_OK;
+}
+int read_scalar(tg_lattice* L, const double* d, double* h) {
+  TG_CK(cudaMemcpyAsync(h, d, sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  return TG_OK;
+}
+int upload_mask(tg_lattice* L, const int* mask) {
+  TG_CK(cudaMemcpyAsync(L->mask, mask, sizeof(int) * L->V, cudaMemcpyHostToDevice, L->stream));
+  return TG_OK;
+}
+}  // namespace
+
+int tg_magnetisation(tg_lattice* L, double* M) {
+  if (!L || !M) return fail(TG_E_ARG, "null argument");
+  sum_links(L->stream, L->g, L->A, &L->ts->Sg0, L->red);
+  TG_CK(cudaGetLastError());
+  double s = 0;
+  TG_TRY(read_scalar(L, &L->ts->Sg0, &s));
+  *M = s / L->V;
+  return TG_OK;
+}
+
+int tg_fermion_phase(tg_lattice* L, int sources, const double* noise, double* phase) {
+  if (!L || !phase || sources <= 0) return fail(TG_E_ARG, "bad argument");
+  const size_t V = (size_t)L->V;
+  std::vector<double> draw;
+  if (!noise) {  // the reference's stream: V Gaussian pairs per source (hmc.c:802)
+    draw.resize(2 * V);
+  }
+  TG_CK(cudaMemsetAsync(&L->ts->Smd1, 0, sizeof(double), L->stream));
+  for (int k = 0; k < sources; k++) {
+    const double* src = noise ? noise + 2 * V * k : nullptr;
+    if (!noise) {
+      L->mt.gauss_pairs((long)V, draw.data());
+      src = draw.data();
+    }
+    TG_TRY(upload(L, L->vin, src, 2 * V));
+    dslash64(L->stream, L->g, op_k(L, 1), 1, L->vin, L->vout, L->Wt, L->Wx);
+    imdot(L->stream, L->g, L->vin, L->vout, &L->ts->Smd1, 1, L->red);
+    TG_CK(cudaGetLastError());
+  }
+  double s = 0;
+  TG_TRY(read_scalar(L, &L->ts->Smd1, &s));
+  *phase = s / sources;
+  return TG_OK;
+}
+
+int tg_chiral_condensate(tg_lattice* L, const tg_cg_params* cp, int sources, unsigned long long seed, double* pbp,
+                         double* err) {
+  if (!L || !pbp || sources <= 0) return fail(TG_E_ARG, "bad argument");
+  TG_TRY(check_cg_params(cp));
+  std::vector<double> vals(sources);
+  for (int k = 0; k < sources; k++) {
+    philox_gauss(L->stream, L->g, seed, L->ts, 64u + (unsigned)k, L->vin);    // eta
+    dslash64(L->stream, L->g, op_k(L, 1), 1, L->vin, L->Mchi, L->Wt, L->Wx);  // M^dag eta
+    TG_CK(cudaGetLastError());
+    tg_cg_result r{};
+    TG_TRY(solve_dev(L, *cp, L->Mchi, L->chi, &r));                         // M^-1 eta
+    if (r.status != TG_OK) return solver_status(r.status);
+    redot(L->stream, L->g, L->vin, L->chi, &L->ts->Smd1, 0, L->red);
+    TG_CK(cudaGetLastError());
+    TG_TRY(read_scalar(L, &L->ts->Smd1, &vals[k]));
+    vals[k] /= 2.0 * L->V;  // E[eta eta^dag] = 2 for complex Gaussian noise of unit-variance parts
+  }
+  double mean = 0;
+  for (double v : vals) mean += v;
+  mean /= sources;
+  double var = 0;
+  for (double v : vals) var += (v - mean) * (v - mean);
+  *pbp = mean;
+  if (err) *err = sources > 1 ? sqrt(var / (sources - 1) / sources) : 0.0;
+  return TG_OK;
+}
+
+int tg_fm_apply(tg_lattice* L, const int* mask, const double* in, double* out, int transpose) {
+  if (!L || !mask || !in || !out) return fail(TG_E_ARG, "null argument");
+  TG_TRY(ensure_real(L));
+  TG_TRY(upload_mask(L, mask));
+  TG_TRY(upload(L, L->rv[0], in, (size_t)L->V));
+  fm_apply(L->stream, L->g, L->P.m, L->P.mu, L->P.bc_t, L->P.bc_x, L->mask, L->rv[0], L->rv[1], transpose);
+  TG_CK(cudaGetLastError());
+  return download(L, out, L->rv[1], (size_t)L->V);
+}
+
+int tg_cg_mdm_masked(tg_lattice* L, const tg_cg_params* cp, const int* mask, const double* b, double* x,
+                     tg_cg_result* res) {
+  if (!L || !mask || !b || !x) return fail(TG_E_ARG, "null argument");
+  TG_TRY(check_cg_params(cp));
+  TG_TRY(ensure_real(L));
+  TG_TRY(upload_mask(L, mask));
+  TG_TRY(upload(L, L->rv[0], b, (size_t)L->V));
+  rcg_init(L->stream, L->g, L->rv[0], L->rv[1], L->rv[2], L->rv[3], cp->rel_tol, cp->abs_tol2, cp->maxiter, L->st,
+           L->red);
+  TG_CK(cudaGetLastError());
+  const int chunk = 16;
+  const long max_chunks = (long)cp->maxiter / chunk + 2;
+  for (long c = 0;; c++) {
+    TG_CK(cudaMemcpyAsync(L->h_st, L->st, sizeof(CgState), cudaMemcpyDeviceToHost, L->stream));
+    TG_CK(cudaStreamSynchronize(L->stream));
+    if (L->h_st->done) break;
+    if (c >= max_chunks) return fail(TG_E_NOCONV, "CG loop did not terminate");
+    for (int j = 0; j < chunk; j++)
+      rcg_iter(L->stream, L->g, L->P.m, L->P.mu, L->P.bc_t, L->P.bc_x, L->mask, L->rv[1], L->rv[2], L->rv[3],
+               L->rv[4], L->rv[5], L->st, L->red);
+    TG_CK(cudaGetLastError());
+  }
+  if (res) {
+    res->iterations = L->h_st->iter;
+    res->status = L->h_st->status;
+    res->reliable_updates = 0;
+    res->rr = L->h_st->rr;
+    res->rr0 = L->h_st->rr0;
+  }
+  TG_TRY(download(L, x, L->rv[1], (size_t)L->V));
+  return solver_status(L->h_st->status);
 }
 
 int tg_trajectory(tg_lattice* L, const tg_hmc_params* p, tg_traj_result* r) {

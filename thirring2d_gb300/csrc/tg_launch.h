@@ -87,6 +87,16 @@ void accept_copy(cudaStream_t s, const Geo& g, const TrajStats* ts, double2* A, 
 // one pure-gauge Metropolis sweep over the 2V links; u[4V]; c = -Nf/g
 void puregauge(cudaStream_t s, const Geo& g, double* A, const double* u, double c);
 
+// Measurements and the masked real operator (tg_aux.cu)
+void sum_links(cudaStream_t s, const Geo& g, const double2* A, double* dst, const Red& red);
+void imdot(cudaStream_t s, const Geo& g, const double2* u, const double2* v, double* dst, int acc, const Red& red);
+void fm_apply(cudaStream_t s, const Geo& g, double m, double mu, int bc_t, int bc_x, const int* mask,
+              const double* in, double* out, int transpose);
+void rcg_init(cudaStream_t s, const Geo& g, const double* b, double* x, double* r, double* p, double rel_tol,
+              double abs_tol2, int maxiter, CgState* st, const Red& red);
+void rcg_iter(cudaStream_t s, const Geo& g, double m, double mu, int bc_t, int bc_x, const int* mask, double* x,
+              double* r, double* p, double* tmp, double* Ap, CgState* st, const Red& red);
+
 // Explicit-grid launchers used by the allocation-free CG entry point.
 int resident_grid_nocache(const void* kernel, int work);
 void link_phase_fixed(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,

@@ -167,6 +167,42 @@ class Lattice:
     def gauge_step(self, mom, eps):
         N.check(self.lib.tg_gauge_step(self.h, _p(_f64(mom)), eps))
 
+    # -- measurements (hmc.c:794-842) ----------------------------------------
+    def magnetisation(self) -> float:
+        v = C.c_double()
+        N.check(self.lib.tg_magnetisation(self.h, C.byref(v)))
+        return v.value
+
+    def fermion_phase(self, sources: int = 20, noise=None) -> float:
+        """hmc.c:794-815; noise [sources, nt, nx] or None (the reference MT stream)."""
+        nz = _c128(np.asarray(noise).reshape(sources, self.nt, self.nx)) if noise is not None else None
+        v = C.c_double()
+        N.check(self.lib.tg_fermion_phase(self.h, sources, _p(nz) if nz is not None else None, C.byref(v)))
+        return v.value
+
+    def chiral_condensate(self, sources: int = 16, seed: int = 0, cp: N.CgParams | None = None):
+        v, e = C.c_double(), C.c_double()
+        N.check(self.lib.tg_chiral_condensate(self.h, C.byref(cp or cg_params(rel_tol=1e-10, abs_tol2=0.0)), sources,
+                                              seed, C.byref(v), C.byref(e)))
+        return v.value, e.value
+
+    # -- fermion-bag operator (vec_ops.c:96-307) ------------------------------
+    def fM(self, mask, v, transpose=False) -> np.ndarray:
+        mask = np.ascontiguousarray(mask, dtype=np.int32).reshape(self.nt, self.nx)
+        v = _f64(v).reshape(self.nt, self.nx)
+        out = np.empty_like(v)
+        N.check(self.lib.tg_fm_apply(self.h, mask.ctypes.data_as(C.POINTER(C.c_int)), _p(v), _p(out), int(transpose)))
+        return out
+
+    def cg_MdM(self, mask, b, cp: N.CgParams | None = None):
+        mask = np.ascontiguousarray(mask, dtype=np.int32).reshape(self.nt, self.nx)
+        b = _f64(b).reshape(self.nt, self.nx)
+        x = np.empty_like(b)
+        res = N.CgResult()
+        N.check(self.lib.tg_cg_mdm_masked(self.h, C.byref(cp or cg_params(maxiter=10000)),
+                                          mask.ctypes.data_as(C.POINTER(C.c_int)), _p(b), _p(x), C.byref(res)), True)
+        return x, res
+
     # -- random numbers and trajectories --------------------------------------
     def seed_mersenne(self, seed: int, warmup: int = 543210):
         N.check(self.lib.tg_mt_seed(self.h, seed, warmup))

@@ -100,6 +100,11 @@ SIGNATURES = {
     "tg_puregauge_ext": (C.c_int, [_vp, _dp, C.c_int]),
     "tg_trajectory": (C.c_int, [_vp, C.POINTER(HmcParams), C.POINTER(TrajResult)]),
     "tg_trajectory_ext": (C.c_int, [_vp, C.POINTER(HmcParams), _dp, _dp, _dp, C.c_double, C.POINTER(TrajResult)]),
+    "tg_magnetisation": (C.c_int, [_vp, _dp]),
+    "tg_fermion_phase": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+    "tg_chiral_condensate": (C.c_int, [_vp, C.POINTER(CgParams), C.c_int, C.c_ulonglong, _dp, _dp]),
+    "tg_fm_apply": (C.c_int, [_vp, C.POINTER(C.c_int), _dp, _dp, C.c_int]),
+    "tg_cg_mdm_masked": (C.c_int, [_vp, C.POINTER(CgParams), C.POINTER(C.c_int), _dp, _dp, C.POINTER(CgResult)]),
     "tg_cg_noalloc": (C.c_int, [C.POINTER(LatticeParams), C.POINTER(CgParams), _vp, _vp, _vp, C.POINTER(CgResult),
                                 _vp]),
     "tg_batch_create": (C.c_int, [C.POINTER(ChainParams), C.c_int, C.c_int, C.POINTER(_vp)]),
