@@ -11,7 +11,7 @@ Workload (one "step" = one HMC trajectory of the hot path):
 Output: one JSON line (rank 0).  `value` is device-timed trajectories/s with the
 gauge field resident in HBM; `e2e` the same through the public C ABI with the
 gauge field uploaded from and downloaded to host memory every trajectory.
-`roofline` is the CG iteration (k_cg1 + k_cg2_64 + k_cg3, >90% of the device
+`roofline` is the CG iteration (k_cg1 + k_cg2_64, >99% of the device
 time), timed with CUDA events inside the trajectory graph, against the
 algorithmic 208 B/site of one FP64 CG iteration.  Also reported: the operator
 apply alone (20 M and 20 M^dag applies, 64 B/site) and the same trajectories
@@ -66,7 +66,7 @@ CG_ITER_DRAM_BYTES = 178.95e6
 # FP64 work of one CG iteration per site, in flops (FMA = 2): two operator
 # applies (16 FMA + 2 MUL each), p' = r + beta p, x/r updates, two norms.
 CG_ITER_FP64_FLOPS_PER_SITE = 2 * 34 + 4 + 8 + 4 + 4
-FP64_PEAK_TFLOPS_NOMINAL = 1.25  # GB300 FP64 (vector) nominal; not in the measured peaks file
+FP64_PEAK_TFLOPS_NOMINAL = 1.25  # GB300 FP64 (vector) nominal, used if the probe cannot run
 
 
 class Clocks:
@@ -309,7 +309,15 @@ def run_ours(args, ws, rank, local):
     hbm, peak_kind = peaks()
     t_iter_ms = cg_ms / max(1, iters)
     achieved = CG_ITER_BYTES_PER_SITE * V / (t_iter_ms * 1e-3) / 1e9
-    launches = sum(1 + 3 * r.cg_iterations for r in res) + args.steps * (3 * W["nsteps"] + 20)
+    # two kernels per CG iteration, an init and at most one early-exit pair per
+    # solve, four kernels per MD step, about 20 for the heatbath and the sums
+    launches = sum(2 * r.cg_iterations + 3 * r.cg_solves for r in res) + args.steps * (4 * W["nsteps"] + 20)
+
+    fp64_achieved = CG_ITER_FP64_FLOPS_PER_SITE * V / (t_iter_ms * 1e-3) / 1e12
+    try:
+        fp64_peak, fp64_peak_kind = tg.native.fp64_peak_tflops(local), "measured (tg_measure_fp64_peak, FMA chains)"
+    except Exception:
+        fp64_peak, fp64_peak_kind = FP64_PEAK_TFLOPS_NOMINAL, "nominal"
 
     if rank != 0:
         return
@@ -321,15 +329,14 @@ def run_ours(args, ws, rank, local):
         "config": config_block(),
         "e2e": {"value": e2e_value, "unit": "trajectories/s", "h2d_bytes_per_step": 16 * V,
                 "d2h_bytes_per_step": 16 * V + 128},
-        "roofline": {"kernel": "CG iteration (k_cg1 + k_cg2_64 + k_cg3), FP64", "bound": "hbm",
+        "roofline": {"kernel": "CG iteration (k_cg1 + k_cg2_64), FP64", "bound": "hbm",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": peak_kind, "bytes_per_site": CG_ITER_BYTES_PER_SITE,
                      "ms_per_iteration": t_iter_ms,
                      "traffic": CG_ITER_DRAM_BYTES,
                      "traffic_source": "profiles/cg_iteration_1024_fp64.md (ncu, one capture)"},
-        "fp64_alu": {"achieved_tflops": CG_ITER_FP64_FLOPS_PER_SITE * V / (t_iter_ms * 1e-3) / 1e12,
-                     "peak_tflops": FP64_PEAK_TFLOPS_NOMINAL, "peak_source": "nominal",
-                     "frac": CG_ITER_FP64_FLOPS_PER_SITE * V / (t_iter_ms * 1e-3) / 1e12 / FP64_PEAK_TFLOPS_NOMINAL,
+        "fp64_alu": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak, "peak_source": fp64_peak_kind,
+                     "frac": fp64_achieved / fp64_peak, "flops_per_site": CG_ITER_FP64_FLOPS_PER_SITE,
                      "note": "the FP64 CG kernels keep the FP64 pipe 85-89% busy (ncu); they are FP64-ALU-bound"},
         "dslash": {"fp64_gbs": dslash_gbs, "fp64_ms_M": t_M, "fp64_ms_Mdag": t_Md, "fp64_frac": dslash_gbs / hbm,
                    "fp32_gbs": dslash32_gbs, "fp32_ms": t_M32, "bytes_per_site_fp64": 64, "bytes_per_site_fp32": 32},
@@ -370,6 +377,9 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
     first_m, first_64 = Bm.trajectory(bpm), B64.trajectory(bp64)   # same fields, same Philox stream
     dh_err = max(abs(a.dH - b.dH) / max(1.0, abs(b.dH)) for a, b in zip(first_m, first_64))
     acc_mismatch = sum(a.accepted != b.accepted for a, b in zip(first_m, first_64))
+    # chains whose MD is stable at this step size (|dH| < 5): the absolute dH error there
+    stable = [(a, b) for a, b in zip(first_m, first_64) if abs(b.dH) < 5.0]
+    dh_err_stable = max((abs(a.dH - b.dH) for a, b in stable), default=0.0)
     B64.close()
     steps = max(1, args.steps)
     ms = 0.0
@@ -404,6 +414,7 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
                                 "sample": f"{sample} of the {nchains} chains, one at a time, second trajectory each"},
             "speedup_vs_sequential_fp64": batched_rate / seq_rate,
             "dH_rel_err_vs_fp64_batch_max": dh_err, "accept_mismatch_vs_fp64": acc_mismatch,
+            "stable_chains": len(stable), "dH_abs_err_vs_fp64_stable_chains_max": dh_err_stable,
             "acceptance": float(np.mean([r.accepted for r in res[-1]])),
             "cg_iterations_per_chain_traj": float(np.mean([r.cg_iterations for r in res[-1]]))}
 

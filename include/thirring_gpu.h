@@ -200,6 +200,23 @@ int tg_fermion_phase(tg_lattice* L, int sources, const double* noise, double* ph
 int tg_chiral_condensate(tg_lattice* L, const tg_cg_params* cp, int sources, unsigned long long seed, double* pbp,
                          double* err);
 
+/* ---- measurement utility (no reference counterpart) ---------------------- */
+/* FP64 FMA throughput of `device` in TFLOP/s (2 flops per FMA; best of 5
+ * timed launches of a kernel of independent FMA chains, CUDA events).  The
+ * FP64 roof against which the FP64 operator and CG kernels are reported. */
+int tg_measure_fp64_peak(int device, double* tflops);
+
+/* ---- dense matrix and determinant (tiny lattices) ------------------------ */
+/* fermion_matrix (hmc.c:269-310) for the lattice's gauge field, row-major
+ * complex: Md[(i*V + j)*2 + {0,1}] = M_ij with (M psi)_i = sum_j M_ij psi_j.
+ * (The reference stores the same elements column-major for LAPACK.)  V <= 4096. */
+int tg_dense_M(tg_lattice* L, double* Md);
+/* determinant (hmc.c:314-336) as log|det M| and arg det M in (-pi, pi], for
+ * nconf gauge fields A (double[nconf*V*2], or NULL for the lattice's own) by
+ * one GPU LU factorisation with partial pivoting per field.  V <= 1024.
+ * Leaves the lattice's gauge field at the last A. */
+int tg_log_det(tg_lattice* L, int nconf, const double* A, double* logabs, double* phase);
+
 /* ---- fermion-bag operator (vec_ops.c) ------------------------------------ */
 /* fM / fM_transpose (vec_ops.c:96-174): the real, gauge-field-free staggered
  * operator with occupied sites (mask[s] != 0) acting as the identity and

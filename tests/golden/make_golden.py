@@ -126,9 +126,30 @@ def make_vecops():
                             fM_v=ref.fM(v), fMt_v=ref.fM(v, True), cg_x=ref.cg_MdM(b))
 
 
+def make_free_det():
+    """The free (A = 0, no monomers) fermion-bag matrix, built column by column
+    from the reference's own vec_ops.c fM, and its log-determinant: the A = 0
+    pin of the determinant (fermion_matrix.c:28-64 fM_index, same operator)."""
+    from oracle.oracle import RefVecOps
+    for name in ("vecops_8x8", "vecops_6x4"):
+        nt, nx, m, mu = VEC_CONFIGS[name][:4]
+        ref = RefVecOps(nt, nx, m, mu)
+        ref.set_field(np.zeros((nt, nx), np.int32))
+        V = nt * nx
+        Mf = np.empty((V, V))
+        for j in range(V):
+            e = np.zeros(V)
+            e[j] = 1.0
+            Mf[:, j] = ref.fM(e.reshape(nt, nx)).ravel()
+        sign, logabs = np.linalg.slogdet(Mf)
+        np.savez_compressed(os.path.join(OUT, f"free_det_{nt}x{nx}.npz"), nt=nt, nx=nx, m=m, mu=mu, M=Mf,
+                            logabsdet=logabs, sign=sign)
+
+
 if __name__ == "__main__":
     make_ref.build([(c[0], c[1]) for c in CONFIGS.values()] + [(4, 4), (6, 4)])
     make_vecops()
+    make_free_det()
     make_mt()
     make_dense()
     for name, cfg in CONFIGS.items():

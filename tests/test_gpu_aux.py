@@ -69,3 +69,41 @@ def test_chiral_condensate_against_exact_trace(tg, oracle_lib):
     o = oracle_lib.Oracle(nt, nx, m, 0.5, 0.0, -1, 1)
     exact = float(np.trace(np.linalg.inv(o.dense_M(A))).real) / (nt * nx)
     assert err > 0 and abs(pbp - exact) < 5 * err, (pbp, exact, err)
+
+
+@pytest.mark.parametrize("name", ["det_4x4_apx", "det_4x4_px", "det_6x4_apx"])
+def test_dense_matrix_and_determinant_golden(tg, name):
+    """fermion_matrix / determinant (hmc.c:269-336) against the reference's
+    dense matrix and numpy's log-determinant of it."""
+    d = golden(name)
+    L = tg.Lattice(int(d["nt"]), int(d["nx"]), float(d["m"]), 0.5, float(d["mu"]), -1, int(d["bc_x"]))
+    L.set_gauge(d["A"])
+    assert np.abs(L.fermion_matrix() - d["M"]).max() < 1e-15
+    la, ph = L.log_det()
+    assert abs(la - float(d["logabsdet"])) < 1e-12
+    assert abs(np.exp(1j * ph) - complex(d["phase"])) < 1e-12
+
+
+def test_batched_determinant_vs_numpy(tg, oracle_lib):
+    nt, nx, m, mu = 8, 8, 0.2, 0.3
+    rng = np.random.default_rng(6)
+    As = rng.normal(0, 0.6, (12, nt, nx, 2))
+    As[0] = 0.0   # A = 0: the free operator (fermion_matrix.c / full_determinant.c at an empty field)
+    L = tg.Lattice(nt, nx, m, 0.5, mu, -1, -1)
+    la, ph = L.log_det(As)
+    o = oracle_lib.Oracle(nt, nx, m, 0.5, mu, -1, -1)
+    for k, A in enumerate(As):
+        sign, logabs = np.linalg.slogdet(o.dense_M(A))
+        assert abs(la[k] - logabs) < 1e-10 * max(1.0, abs(logabs))
+        assert abs(np.exp(1j * ph[k]) - sign) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["free_det_8x8", "free_det_6x4"])
+def test_free_determinant_golden(tg, name):
+    """log det M at A = 0 against the fermion-bag matrix of the reference's vec_ops.c."""
+    d = golden(name)
+    nt, nx = int(d["nt"]), int(d["nx"])
+    L = tg.Lattice(nt, nx, float(d["m"]), 0.5, float(d["mu"]), -1, -1)
+    la, ph = L.log_det(np.zeros((1, nt, nx, 2)))
+    assert abs(la[0] - float(d["logabsdet"])) < 1e-12
+    assert abs(np.exp(1j * ph[0]) - float(d["sign"])) < 1e-12

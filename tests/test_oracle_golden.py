@@ -123,3 +123,17 @@ def test_masked_operator_oracle(oracle_lib, name):
     assert np.abs(o.fM(d["mask"], d["v"], True) - d["fMt_v"]).max() < 1e-14
     x, st, it = o.cg_MdM(d["mask"], d["b"], maxiter=10000)
     assert st == 0 and rel(x, d["cg_x"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["free_det_8x8", "free_det_6x4"])
+def test_free_matrix_equals_fermion_bag_matrix(oracle_lib, name):
+    """At A = 0 hmc.c's M (antiperiodic t and x) is the fermion-bag matrix of
+    vec_ops.c / fermion_matrix.c:28-64 with no monomers; the fixture holds the
+    latter, built from the reference's own fM."""
+    d = golden(name)
+    nt, nx = int(d["nt"]), int(d["nx"])
+    o = oracle_lib.Oracle(nt, nx, float(d["m"]), 0.5, float(d["mu"]), -1, -1)
+    Md = o.dense_M(np.zeros((nt, nx, 2)))
+    assert np.abs(Md - d["M"]).max() < 1e-15
+    sign, logabs = np.linalg.slogdet(Md)
+    assert abs(logabs - float(d["logabsdet"])) < 1e-12 and abs(sign - float(d["sign"])) < 1e-12

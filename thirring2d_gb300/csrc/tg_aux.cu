@@ -181,3 +181,147 @@ void rcg_iter(cudaStream_t s, const Geo& g, double m, double mu, int bc_t, int b
 }
 
 }  // namespace tg
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// Dense M and its determinant for tiny lattices (fermion_matrix and
+// determinant, hmc.c:269-336).  Row-major: (M psi)_i = sum_j Md[i*V + j] psi_j,
+// the same operator as the stencil (entries accumulate, so sides of 2, whose
+// two neighbours coincide, are built correctly).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_dense_M(Geo g, OpK<double> k, const double2* __restrict__ Wt,
+                                                   const double2* __restrict__ Wx, double2* __restrict__ Md) {
+  const long long V = g.V;
+  TG_SITES(i, g.V) {
+    double2* row = Md + (long long)i * V;
+    for (long long j = 0; j < V; j++) row[j] = make_double2(0, 0);
+    int t, x;
+    site_tx(g, i, t, x);
+    Nbr n = neighbours(g, i, t, x);
+    auto add = [&](int j, double2 v) {
+      row[j].x += v.x;
+      row[j].y += v.y;
+    };
+    add(i, make_double2(k.m, 0));
+    double2 w = Wt[i];
+    add(n.tp, make_double2(k.cf * w.x, k.cf * w.y));         // cf * Wt(s)
+    w = Wt[n.tm];
+    add(n.tm, make_double2(k.cb * w.x, -k.cb * w.y));        // cb * conj(Wt(s-t))
+    w = Wx[i];
+    add(n.xp, w);                                            // + Wx(s)
+    w = Wx[n.xm];
+    add(n.xm, make_double2(-w.x, w.y));                      // - conj(Wx(s-x))
+  }
+}
+
+// LU with partial pivoting of one V x V complex matrix per block (in place).
+// out[2*b] = log|det|, out[2*b+1] = arg(det) in (-pi, pi].
+__global__ void __launch_bounds__(1024) k_lu_logdet(int V, double2* __restrict__ mats, double* __restrict__ out) {
+  double2* a = mats + (long long)blockIdx.x * V * V;
+  __shared__ double s_mag[1024];
+  __shared__ int s_idx[1024];
+  __shared__ int piv;
+  double logabs = 0, ph = 0;  // valid in thread 0
+  for (int k = 0; k < V; k++) {
+    // pivot: largest |a_ik|, i >= k (ties to the smallest index: deterministic)
+    double best = -1;
+    int bi = k;
+    for (int i = k + threadIdx.x; i < V; i += blockDim.x) {
+      double2 v = a[(long long)i * V + k];
+      double mag = v.x * v.x + v.y * v.y;
+      if (mag > best) { best = mag; bi = i; }
+    }
+    s_mag[threadIdx.x] = best;
+    s_idx[threadIdx.x] = bi;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+      if (threadIdx.x < off) {
+        double o = s_mag[threadIdx.x + off];
+        int oi = s_idx[threadIdx.x + off];
+        if (o > s_mag[threadIdx.x] || (o == s_mag[threadIdx.x] && oi < s_idx[threadIdx.x])) {
+          s_mag[threadIdx.x] = o;
+          s_idx[threadIdx.x] = oi;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) piv = s_idx[0];
+    __syncthreads();
+    const int p = piv;
+    if (p != k) {
+      for (int j = threadIdx.x; j < V; j += blockDim.x) {
+        double2 u = a[(long long)k * V + j];
+        a[(long long)k * V + j] = a[(long long)p * V + j];
+        a[(long long)p * V + j] = u;
+      }
+      if (threadIdx.x == 0) ph += M_PI;  // a row swap flips the sign
+    }
+    __syncthreads();
+    const double2 d = a[(long long)k * V + k];
+    if (threadIdx.x == 0) {
+      logabs += 0.5 * log(d.x * d.x + d.y * d.y);
+      ph += atan2(d.y, d.x);
+    }
+    const double inv = 1.0 / (d.x * d.x + d.y * d.y);
+    const double2 dinv = make_double2(d.x * inv, -d.y * inv);
+    // eliminate below the pivot: a_ij -= (a_ik / a_kk) a_kj, i, j > k
+    const int rows = V - k - 1;
+    const long long work = (long long)rows * (V - k);
+    for (long long w = threadIdx.x; w < work; w += blockDim.x) {
+      const int i = k + 1 + (int)(w / (V - k));
+      const int j = k + (int)(w % (V - k));
+      double2 aik = a[(long long)i * V + k];
+      double2 l = cmul<double>(aik, dinv);
+      if (j == k) continue;  // column k is finished after the update below
+      double2 akj = a[(long long)k * V + j];
+      double2& aij = a[(long long)i * V + j];
+      aij.x -= l.x * akj.x - l.y * akj.y;
+      aij.y -= l.x * akj.y + l.y * akj.x;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    ph = remainder(ph, 2 * M_PI);
+    out[2 * blockIdx.x] = logabs;
+    out[2 * blockIdx.x + 1] = ph;
+  }
+}
+
+void dense_M(cudaStream_t s, const Geo& g, const OpK<double>& k, const double2* Wt, const double2* Wx, double2* Md) {
+  k_dense_M<<<nblocks(g.V), kBlock, 0, s>>>(g, k, Wt, Wx, Md);
+}
+void lu_logdet(cudaStream_t s, int V, int nmat, double2* mats, double* out) {
+  k_lu_logdet<<<nmat, 1024, 0, s>>>(V, mats, out);
+}
+
+}  // namespace tg
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// FP64 FMA throughput of this GPU: 8 independent dependent chains per thread,
+// 4 blocks of 256 threads per SM.  The store is conditional on a value the
+// chains never reach, so nothing is eliminated and nothing is written.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_dfma_peak(int iters, double seed, double* sink) {
+  const double b = 0.9999999, c = 1e-9;
+  double a0 = seed + threadIdx.x * 1e-12, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
+  double a4 = a0 + 4e-3, a5 = a0 + 5e-3, a6 = a0 + 6e-3, a7 = a0 + 7e-3;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+      a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+  }
+  const double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == -1.0) sink[0] = s;
+}
+
+// FMA count of one launch: grid * 256 threads * 8 chains * 4 * iters
+void dfma_peak(cudaStream_t s, int grid, int iters, double* sink) {
+  k_dfma_peak<<<grid, 256, 0, s>>>(iters, 1.0, sink);
+}
+
+}  // namespace tg

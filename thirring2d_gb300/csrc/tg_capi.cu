@@ -528,6 +528,43 @@ extern "C" {
 const char* tg_last_error(void) { return g_err.c_str(); }
 const char* tg_version(void) { return "thirring2d_gb300 0.1 (sm_103a)"; }
 
+int tg_measure_fp64_peak(int device, double* tflops) {
+  if (!tflops) return fail(TG_E_ARG, "null argument");
+  TG_CK(cudaSetDevice(device));
+  int sms = 0;
+  TG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int grid = 4 * sms, iters = 2048;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double* sink = nullptr;
+  int rc = TG_OK;
+  float best = 0;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess || cudaMalloc(&sink, sizeof(double)) != cudaSuccess) {
+    rc = fail(TG_E_CUDA, "fp64 peak setup failed");
+  } else {
+    dfma_peak(st, grid, iters, sink);  // warm-up
+    for (int rep = 0; rep < 5 && rc == TG_OK; rep++) {
+      float ms = 0;
+      if (cudaEventRecord(e0, st) != cudaSuccess) rc = TG_E_CUDA;
+      dfma_peak(st, grid, iters, sink);
+      if (rc == TG_OK && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                          cudaGetLastError() != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+        rc = TG_E_CUDA;
+      if (rc == TG_OK && ms > 0 && (best == 0 || ms < best)) best = ms;
+    }
+    if (rc != TG_OK) fail(TG_E_CUDA, "fp64 peak kernel failed");
+  }
+  if (sink) cudaFree(sink);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  if (rc != TG_OK) return rc;
+  const double fmas = (double)grid * 256 * 32 * iters;
+  *tflops = 2.0 * fmas / (best * 1e-3) / 1e12;
+  return TG_OK;
+}
+
 int tg_create(const tg_lattice_params* p, tg_lattice** out) {
   if (!p || !out) return fail(TG_E_ARG, "null argument");
   *out = nullptr;
@@ -1019,6 +1056,52 @@ int tg_cg_mdm_masked(tg_lattice* L, const tg_cg_params* cp, const int* mask, con
   }
   TG_TRY(download(L, x, L->rv[1], (size_t)L->V));
   return solver_status(L->h_st->status);
+}
+
+int tg_dense_M(tg_lattice* L, double* Md) {
+  if (!L || !Md) return fail(TG_E_ARG, "null argument");
+  if (L->V > 4096) return fail(TG_E_ARG, "dense M only for lattices of at most 4096 sites");
+  const size_t n = (size_t)L->V * L->V;
+  double2* d = nullptr;
+  TG_TRY(dmalloc(&d, n));
+  dense_M(L->stream, L->g, op_k(L, 0), L->Wt, L->Wx, d);
+  cudaError_t e1 = cudaGetLastError();
+  cudaError_t e2 = cudaMemcpyAsync(Md, d, n * sizeof(double2), cudaMemcpyDeviceToHost, L->stream);
+  cudaError_t e3 = cudaStreamSynchronize(L->stream);
+  cudaFree(d);
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) return fail(TG_E_CUDA, "dense M failed");
+  return TG_OK;
+}
+
+int tg_log_det(tg_lattice* L, int nconf, const double* A, double* logabs, double* phase) {
+  if (!L || nconf <= 0 || !logabs || !phase) return fail(TG_E_ARG, "bad argument");
+  if (L->V > 1024) return fail(TG_E_ARG, "determinant only for lattices of at most 1024 sites");
+  const size_t V = (size_t)L->V, n = V * V;
+  double2* mats = nullptr;
+  double* out = nullptr;
+  TG_TRY(dmalloc(&mats, n * nconf));
+  if (dmalloc(&out, 2 * (size_t)nconf) != TG_OK) { cudaFree(mats); return TG_E_ALLOC; }
+  int rc = TG_OK;
+  std::vector<double> h(2 * (size_t)nconf);
+  for (int c = 0; c < nconf && rc == TG_OK; c++) {
+    if (A) rc = tg_set_gauge(L, A + 2 * V * c);
+    if (rc == TG_OK) dense_M(L->stream, L->g, op_k(L, 0), L->Wt, L->Wx, mats + n * c);
+  }
+  if (rc == TG_OK) {
+    lu_logdet(L->stream, (int)V, nconf, mats, out);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(h.data(), out, h.size() * sizeof(double), cudaMemcpyDeviceToHost, L->stream) != cudaSuccess ||
+        cudaStreamSynchronize(L->stream) != cudaSuccess)
+      rc = fail(TG_E_CUDA, "determinant kernel failed");
+  }
+  cudaFree(mats);
+  cudaFree(out);
+  if (rc != TG_OK) return rc;
+  for (int c = 0; c < nconf; c++) {
+    logabs[c] = h[2 * c];
+    phase[c] = h[2 * c + 1];
+  }
+  return TG_OK;
 }
 
 int tg_trajectory(tg_lattice* L, const tg_hmc_params* p, tg_traj_result* r) {

@@ -97,6 +97,13 @@ void rcg_init(cudaStream_t s, const Geo& g, const double* b, double* x, double* 
 void rcg_iter(cudaStream_t s, const Geo& g, double m, double mu, int bc_t, int bc_x, const int* mask, double* x,
               double* r, double* p, double* tmp, double* Ap, CgState* st, const Red& red);
 
+void dense_M(cudaStream_t s, const Geo& g, const OpK<double>& k, const double2* Wt, const double2* Wx, double2* Md);
+// log|det| and arg det of nmat V x V complex matrices (overwritten by their LU factors)
+void lu_logdet(cudaStream_t s, int V, int nmat, double2* mats, double* out);
+
+// FP64 FMA throughput probe: grid * 256 * 32 * iters FMAs, writes nothing
+void dfma_peak(cudaStream_t s, int grid, int iters, double* sink);
+
 // Explicit-grid launchers used by the allocation-free CG entry point.
 int resident_grid_nocache(const void* kernel, int work);
 void link_phase_fixed(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,

@@ -186,6 +186,24 @@ class Lattice:
                                               seed, C.byref(v), C.byref(e)))
         return v.value, e.value
 
+    # -- dense matrix and determinant (hmc.c:269-336) -------------------------
+    def fermion_matrix(self) -> np.ndarray:
+        out = np.empty((self.V, self.V), np.complex128)
+        N.check(self.lib.tg_dense_M(self.h, _p(out)))
+        return out
+
+    def log_det(self, A_batch=None):
+        """(log|det M|, arg det M) per gauge field of A_batch [n, nt, nx, 2] (None: the current field)."""
+        if A_batch is None:
+            la, ph = C.c_double(), C.c_double()
+            N.check(self.lib.tg_log_det(self.h, 1, None, C.byref(la), C.byref(ph)))
+            return la.value, ph.value
+        A_batch = _f64(A_batch).reshape(-1, self.nt, self.nx, 2)
+        n = len(A_batch)
+        la, ph = np.empty(n), np.empty(n)
+        N.check(self.lib.tg_log_det(self.h, n, _p(A_batch), _p(la), _p(ph)))
+        return la, ph
+
     # -- fermion-bag operator (vec_ops.c:96-307) ------------------------------
     def fM(self, mask, v, transpose=False) -> np.ndarray:
         mask = np.ascontiguousarray(mask, dtype=np.int32).reshape(self.nt, self.nx)

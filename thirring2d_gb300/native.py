@@ -103,6 +103,9 @@ SIGNATURES = {
     "tg_magnetisation": (C.c_int, [_vp, _dp]),
     "tg_fermion_phase": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "tg_chiral_condensate": (C.c_int, [_vp, C.POINTER(CgParams), C.c_int, C.c_ulonglong, _dp, _dp]),
+    "tg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
+    "tg_dense_M": (C.c_int, [_vp, _dp]),
+    "tg_log_det": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
     "tg_fm_apply": (C.c_int, [_vp, C.POINTER(C.c_int), _dp, _dp, C.c_int]),
     "tg_cg_mdm_masked": (C.c_int, [_vp, C.POINTER(CgParams), C.POINTER(C.c_int), _dp, _dp, C.POINTER(CgResult)]),
     "tg_cg_noalloc": (C.c_int, [C.POINTER(LatticeParams), C.POINTER(CgParams), _vp, _vp, _vp, C.POINTER(CgResult),
@@ -145,3 +148,10 @@ def check(rc: int, allow_solver_status: bool = False) -> int:
         return rc
     msg = load().tg_last_error()
     raise TGError(rc, msg.decode() if msg else "")
+
+
+def fp64_peak_tflops(device: int = 0) -> float:
+    """Measured FP64 FMA throughput of the GPU (TFLOP/s, tg_measure_fp64_peak)."""
+    v = C.c_double()
+    check(load().tg_measure_fp64_peak(device, C.byref(v)))
+    return v.value

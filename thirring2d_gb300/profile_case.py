@@ -22,7 +22,7 @@ from .lattice import Lattice, cg_params
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--size", type=int, default=1024, help="lattice side (the C3 report uses 2048)")
     ap.add_argument("--iters", type=int, default=100)
     ap.add_argument("--applies", type=int, default=20)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
@@ -31,11 +31,15 @@ def main():
     ap.add_argument("--trajectories", type=int, default=2)
     ap.add_argument("--sequential", type=int, default=0, help="chains to also run one at a time (FP64 path)")
     ap.add_argument("--c5", action="store_true", help="the 64^2 differentiation / dH-scaling report")
+    ap.add_argument("--c3", action="store_true", help="the 2048^2 ill-conditioned mixed-precision report")
+    ap.add_argument("--c3-tau", type=float, nargs="+", default=[1.0, 0.05], help="trajectory lengths of the C3 report")
     a = ap.parse_args()
     if a.batch:
         return batch_case(a)
     if a.c5:
         return c5_case(a)
+    if a.c3:
+        return c3_case(a)
     n = a.size
     rng = np.random.default_rng(n)
     L = Lattice(n, n, 0.05, 0.6, 0.0, N.BC_ANTIPERIODIC, N.BC_PERIODIC)
@@ -137,6 +141,65 @@ def c5_case(a):
         row["accept_mismatch"] = int(sum(x != y for x, y in zip(dhs["fp64"][1], dhs["mixed"][1])))
         out["rows"].append(row)
         print(json.dumps(row), flush=True)
+    print(json.dumps(out))
+
+
+def c3_case(a):
+    """2048^2 (a.size), m 0.02, g 0.8, A ~ N(0, 0.5^2): one CG solve of M^dag M x = b
+    to relative residual 1e-10 in FP64 and in FP32 with FP64 reliable updates
+    every 50 iterations (iterations, wall time, true residual, distance between
+    the two solutions), then a.trajectories trajectories of 30 leapfrog steps in
+    each precision on the same Philox stream (dH per trajectory and their
+    difference)."""
+    import time
+
+    from .lattice import hmc_params
+    n, m, g = a.size, 0.02, 0.8
+    rng = np.random.default_rng(2048)
+    A0 = rng.normal(0, 0.5, (n, n, 2))
+    b = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    out = {"lattice": f"{n}x{n}", "m": m, "g": g, "solve": {}, "trajectories": []}
+    L = Lattice(n, n, m, g, 0.0, N.BC_ANTIPERIODIC, N.BC_PERIODIC)
+    L.set_gauge(A0)
+    xs = {}
+    for prec, name in ((N.PREC_FP64, "fp64"), (N.PREC_MIXED, "mixed")):
+        cp = cg_params(rel_tol=1e-10, abs_tol2=0.0, maxiter=200000, precision=prec, ru_interval=50)
+        L.fmdm_invert_cg(b, cp)  # warm-up (graph instantiation)
+        t0 = time.perf_counter()
+        x, res = L.fmdm_invert_cg(b, cp)
+        ms = 1e3 * (time.perf_counter() - t0)
+        true_res = float(np.linalg.norm(b - L.fm_conjugate_mul(L.fm_mul(x))) / np.linalg.norm(b))
+        xs[name] = x
+        out["solve"][name] = {"iterations": res.iterations, "reliable_updates": res.reliable_updates,
+                              "status": N.STATUS_NAMES[res.status], "ms": ms, "true_rel_residual": true_res}
+    out["solve"]["rel_diff_mixed_vs_fp64"] = float(np.linalg.norm(xs["mixed"] - xs["fp64"]) / np.linalg.norm(xs["fp64"]))
+    print(json.dumps(out["solve"]), flush=True)
+    L.close()
+    # tau 1 is the configuration as specified (30 steps of 1/30: the MD is
+    # unstable there, |dH| ~ 1e12); tau 0.05 (30 steps of 1/600) is a step
+    # size at which it is stable, so the dH difference measures the solver
+    for tau in a.c3_tau:
+        runs = {}
+        for prec, name in ((N.PREC_FP64, "fp64"), (N.PREC_MIXED, "mixed")):
+            L = Lattice(n, n, m, g, 0.0, N.BC_ANTIPERIODIC, N.BC_PERIODIC)
+            L.set_gauge(A0)
+            hp = hmc_params(nsteps=30, tau=tau, rng=N.RNG_PHILOX, seed=3,
+                            cg=cg_params(rel_tol=1e-10, abs_tol2=0.0, maxiter=200000, precision=prec, ru_interval=50))
+            rs = []
+            for _ in range(a.trajectories):
+                t0 = time.perf_counter()
+                r = L.update_gauge(hp)
+                rs.append((r.dH, r.accepted, r.status, r.cg_iterations, r.cg_solves, time.perf_counter() - t0))
+            runs[name] = rs
+            L.close()
+        for k in range(a.trajectories):
+            f, x = runs["fp64"][k], runs["mixed"][k]
+            row = {"tau": tau, "traj": k, "dH_fp64": f[0], "dH_mixed": x[0], "abs_diff": abs(f[0] - x[0]),
+                   "rel_diff": abs(f[0] - x[0]) / max(1.0, abs(f[0])), "accepted": [f[1], x[1]],
+                   "status": [N.STATUS_NAMES[f[2]], N.STATUS_NAMES[x[2]]], "cg_iterations": [f[3], x[3]],
+                   "cg_solves": [f[4], x[4]], "s": [f[5], x[5]]}
+            out["trajectories"].append(row)
+            print(json.dumps(row), flush=True)
     print(json.dumps(out))
 
 
