@@ -201,8 +201,9 @@ int tg_chiral_condensate(tg_lattice* L, const tg_cg_params* cp, int sources, uns
                          double* err);
 
 /* ---- measurement utility (no reference counterpart) ---------------------- */
-/* FP64 FMA throughput of `device` in TFLOP/s (2 flops per FMA; best of 5
- * timed launches of a kernel of independent FMA chains, CUDA events).  The
+/* FP64 FMA throughput of `device` in TFLOP/s (2 flops per FMA; the best of
+ * timed launches of a kernel of independent FMA chains at 2, 4 and 8 blocks of
+ * 256 threads per SM, CUDA events).  The
  * FP64 roof against which the FP64 operator and CG kernels are reported. */
 int tg_measure_fp64_peak(int device, double* tflops);
 

@@ -114,6 +114,28 @@ def test_cg_iterations_match_oracle(tg, oracle_lib):
         assert rel(x, xo) < 50 * tol
 
 
+@pytest.mark.parametrize("m,mu", [(0.0, 0.0), (0.3, 0.0), (0.3, 0.25)])
+def test_cg_mass_forms(tg, oracle_lib, m, mu):
+    """For m != 0 the FP64 CG iterates on (M/m)^dag (M/m) with links W/m
+    (same residuals and stopping test as hmc.c:341-404); m = 0 keeps the plain
+    form.  Both against the oracle's CG; the lattice is created at another mass
+    so the W/m links must follow tg_set_couplings."""
+    rng = np.random.default_rng(21)
+    nt, nx = 16, 32   # column-march stencil path
+    A = rng.normal(0, 0.5, (nt, nx, 2))
+    b = cplx(rng, (nt, nx))
+    L = tg.Lattice(nt, nx, 0.7, 0.5, 0.0, -1, 1)
+    L.set_gauge(A)
+    L.set_couplings(m, 0.5, mu)
+    o = oracle_lib.Oracle(nt, nx, m, 0.5, mu, -1, 1)
+    x, res = L.fmdm_invert_cg(b, tg.cg_params(rel_tol=1e-12, abs_tol2=0))
+    xo, st, it = o.cg(A, b, rel_tol=1e-12, abs_tol2=0)
+    assert res.status == 0 and st == 0
+    assert abs(res.iterations - it) <= 2
+    assert rel(x, xo) < 1e-10
+    assert rel(L.fm_mul(b), o.M(A, b)) < 1e-13
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_cg_true_residual_1024(tg, oracle_lib, precision):
     """The 1024^2 workload (m=0.05, g=0.6, A ~ N(0, 0.3^2)): CG to 1e-10 relative,

@@ -16,8 +16,8 @@ namespace tg {
 // eta_t(x) = (-1)^x, eta_x = 1 (hmc.c:914-921); bc_mu applies on the link that
 // leaves the last slice (hmc.c:143-148, 165-170).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void write_links(const Geo& g, int bc_t, int bc_x, int s, double2 a, double2* Wt,
-                                            double2* Wx, float2* Wt32, float2* Wx32) {
+__device__ __forceinline__ void link_vals(const Geo& g, int bc_t, int bc_x, int s, double2 a, double2& wt,
+                                          double2& wx) {
   int t, x;
   site_tx(g, s, t, x);
   double ft = 0.5 * ((x & 1) ? -1.0 : 1.0) * ((t == g.nt - 1) ? (double)bc_t : 1.0);
@@ -25,25 +25,47 @@ __device__ __forceinline__ void write_links(const Geo& g, int bc_t, int bc_x, in
   double st, ct, sx, cx;
   sincos(a.x, &st, &ct);
   sincos(a.y, &sx, &cx);
-  double2 wt = make_double2(ft * ct, ft * st);
-  double2 wx = make_double2(fx * cx, fx * sx);
+  wt = make_double2(ft * ct, ft * st);
+  wx = make_double2(fx * cx, fx * sx);
+}
+
+__device__ __forceinline__ void write_links(const Geo& g, int bc_t, int bc_x, int s, double2 a, double2* Wt,
+                                            double2* Wx, float2* Wt32, float2* Wx32) {
+  double2 wt, wx;
+  link_vals(g, bc_t, bc_x, s, a, wt, wx);
   Wt[s] = wt;
   Wx[s] = wx;
   Wt32[s] = make_float2((float)wt.x, (float)wt.y);
   Wx32[s] = make_float2((float)wx.x, (float)wx.y);
 }
 
+// ... and W / m for the unit-mass operator M / m = 1 + D / m when o.Wt1 is set
+__device__ __forceinline__ void write_links(const Geo& g, int bc_t, int bc_x, int s, double2 a, const LinkOut& o) {
+  double2 wt, wx;
+  link_vals(g, bc_t, bc_x, s, a, wt, wx);
+  o.Wt[s] = wt;
+  o.Wx[s] = wx;
+  o.Wt32[s] = make_float2((float)wt.x, (float)wt.y);
+  o.Wx32[s] = make_float2((float)wx.x, (float)wx.y);
+  if (o.Wt1 != nullptr) {
+    o.Wt1[s] = make_double2(wt.x * o.inv_m, wt.y * o.inv_m);
+    o.Wx1[s] = make_double2(wx.x * o.inv_m, wx.y * o.inv_m);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // The staggered operator at one site: hmc.c:132-183 for M (DAG = 0) and the
 // true adjoint M^dagger = m - D(-mu) (DAG = 1).  MU0 drops the e^{+-mu}
-// factors (mu = 0): 18 FMA/MUL per site instead of 22.
+// factors (mu = 0): 18 FMA/MUL per site instead of 22.  UNIT applies
+// M / m = 1 + D / m instead (the links passed in are then W / m): the mass
+// product goes, 16 FMA per site.
 // ---------------------------------------------------------------------------
-template <typename R, int DAG, bool MU0>
+template <typename R, int DAG, bool MU0, bool UNIT = false>
 __device__ __forceinline__ C2<R> dslash_vals(const OpK<R>& k, C2<R> pc, C2<R> ptu, C2<R> ptd, C2<R> pxu, C2<R> pxd,
                                              C2<R> wt, C2<R> wtd, C2<R> wx, C2<R> wxd) {
   // pc = in(s); ptu/ptd = in(s+t)/in(s-t); pxu/pxd = in(s+x)/in(s-x);
   // wt = Wt(s), wtd = Wt(s-t), wx = Wx(s), wxd = Wx(s-x)
-  C2<R> o = mk<R>(k.m * pc.x, k.m * pc.y);
+  C2<R> o = UNIT ? pc : mk<R>(k.m * pc.x, k.m * pc.y);
   if (MU0) {
     if (DAG == 0) {
       cmac<R>(o, wt, ptu);

@@ -19,15 +19,15 @@
 namespace tg {
 
 __global__ void __launch_bounds__(kBlock) k_link_phase(Geo g, int bc_t, int bc_x, const double2* __restrict__ A,
-                                                       double2* Wt, double2* Wx, float2* Wt32, float2* Wx32) {
-  TG_SITES(s, g.V) write_links(g, bc_t, bc_x, s, A[s], Wt, Wx, Wt32, Wx32);
+                                                       LinkOut o) {
+  TG_SITES(s, g.V) write_links(g, bc_t, bc_x, s, A[s], o);
 }
 
 // gauge_step (hmc.c:97-101) applied nadd times: A += c*p with c = 2*eps,
 // product then sum (two roundings) as the reference's host code computes it.
 __global__ void __launch_bounds__(kBlock) k_gauge_step(Geo g, int bc_t, int bc_x, double2* A,
                                                        const double2* __restrict__ mom, double c, int nadd,
-                                                       double2* Wt, double2* Wx, float2* Wt32, float2* Wx32) {
+                                                       LinkOut o) {
   TG_SITES(s, g.V) {
     double2 a = A[s];
     double2 p = mom[s];
@@ -36,24 +36,23 @@ __global__ void __launch_bounds__(kBlock) k_gauge_step(Geo g, int bc_t, int bc_x
       a.y = __dadd_rn(a.y, __dmul_rn(c, p.y));
     }
     A[s] = a;
-    write_links(g, bc_t, bc_x, s, a, Wt, Wx, Wt32, Wx32);
+    write_links(g, bc_t, bc_x, s, a, o);
   }
 }
 
-void link_phase(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,
-                float2* Wt32, float2* Wx32) {
-  k_link_phase<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, Wt, Wx, Wt32, Wx32);
+void link_phase(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, const LinkOut& o) {
+  k_link_phase<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, o);
 }
 void gauge_step(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double2* A, const double2* mom, double c,
-                int nadd, double2* Wt, double2* Wx, float2* Wt32, float2* Wx32) {
-  k_gauge_step<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, mom, c, nadd, Wt, Wx, Wt32, Wx32);
+                int nadd, const LinkOut& o) {
+  k_gauge_step<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, mom, c, nadd, o);
 }
 
 // One column-march item: rows t0 .. t0+kMarchT-1 of the 32 columns
 // x = 32*xw + lane.  ld(i) yields the operand at site i (a plain load, or a
 // vector recombined on the fly); epi(s, out(s), operand(s)) consumes each
 // site's result.
-template <typename R, int DAG, bool MU0, class Ld, class Epi>
+template <typename R, int DAG, bool MU0, bool UNIT = false, class Ld, class Epi>
 __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
                                            const C2<R>* __restrict__ Wx, int item, Epi& epi) {
   const int nx = g.nx;
@@ -62,12 +61,21 @@ __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld
   const int xw = item - tb * nxw;
   const int t0 = tb * kMarchT;
   const int lane = threadIdx.x & 31;
-  const int x = (xw << 5) + lane;
-  const int xr = (x + 1 == nx) ? 0 : x + 1;
-  const int xl = (x == 0) ? nx - 1 : x - 1;
-  // the one operand each lane fetches across the warp edge: lane 31 its right
-  // neighbour, lane 0 its left one, the others a duplicate (uniform, no branch)
-  const int xe = (lane == 31) ? xr : xl;
+  const int x0 = xw << 5;
+  const int x = x0 + lane;
+  // The operands across the warp's two edges, fetched once per item by the
+  // first lanes: lane i < kMarchT the operand left of column x0 in row t0+i,
+  // lane kMarchT+i the one right of column x0+31, and lane i < kMarchT also
+  // the x link entering column x0.  Each row hands them to lanes 0 and 31 by
+  // shuffles, so no lane fetches (or recombines) an operand it does not use.
+  const int xle = (x0 == 0) ? nx - 1 : x0 - 1;
+  const int xre = (x0 + 32 == nx) ? 0 : x0 + 32;
+  C2<R> ep = mk<R>(0, 0), ew = mk<R>(0, 0);
+  if (lane < 2 * kMarchT) {
+    const int row = t0 + (lane < kMarchT ? lane : lane - kMarchT);
+    ep = ld(row * nx + (lane < kMarchT ? xle : xre));
+    if (lane < kMarchT) ew = Wx[row * nx + xle];
+  }
   const int tm = (t0 == 0) ? g.nt - 1 : t0 - 1;
   C2<R> pm = ld(tm * nx + x);
   C2<R> wtm = Wt[tm * nx + x];
@@ -80,8 +88,9 @@ __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld
     const C2<R> pp = ld(tp * nx + x);
     const C2<R> wt = Wt[s];
     const C2<R> wx = Wx[s];
-    const C2<R> pe = ld(t * nx + xe);
-    const C2<R> we = Wx[t * nx + xl];
+    const int src = (lane == 31) ? kMarchT + i : i;
+    const C2<R> pe = mk<R>(__shfl_sync(0xffffffffu, ep.x, src), __shfl_sync(0xffffffffu, ep.y, src));
+    const C2<R> we = mk<R>(__shfl_sync(0xffffffffu, ew.x, i), __shfl_sync(0xffffffffu, ew.y, i));
     C2<R> pr = shfl_down1<R>(pc);
     C2<R> pl = shfl_up1<R>(pc);
     C2<R> wl = shfl_up1<R>(wx);
@@ -90,7 +99,7 @@ __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld
       pl = pe;
       wl = we;
     }
-    epi(s, dslash_vals<R, DAG, MU0>(k, pc, pp, pm, pr, pl, wt, wtm, wx, wl), pc);
+    epi(s, dslash_vals<R, DAG, MU0, UNIT>(k, pc, pp, pm, pr, pl, wt, wtm, wx, wl), pc);
     pm = pc;
     pc = pp;
     wtm = wt;
@@ -99,32 +108,32 @@ __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld
 
 // Apply the operator to every site and hand each result to epi: column march
 // where the lattice allows it, else one site per thread.
-template <typename R, int DAG, bool MU0, class Ld, class Epi>
+template <typename R, int DAG, bool MU0, bool UNIT = false, class Ld, class Epi>
 __device__ __forceinline__ void stencil_ld(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
                                            const C2<R>* __restrict__ Wx, Epi& epi) {
   if (g.march) {
     const int items = (g.nx >> 5) * (g.nt / kMarchT);
     constexpr int wpb = kBlock / 32;
     for (int item = blockIdx.x * wpb + (threadIdx.x >> 5); item < items; item += gridDim.x * wpb)
-      march_item<R, DAG, MU0>(g, k, ld, Wt, Wx, item, epi);
+      march_item<R, DAG, MU0, UNIT>(g, k, ld, Wt, Wx, item, epi);
   } else {
     TG_SITES(s, g.V) {
       int t, x;
       site_tx(g, s, t, x);
       const Nbr n = neighbours(g, s, t, x);
       const C2<R> pc = ld(s);
-      epi(s, dslash_vals<R, DAG, MU0>(k, pc, ld(n.tp), ld(n.tm), ld(n.xp), ld(n.xm), Wt[s], Wt[n.tm], Wx[s],
-                                      Wx[n.xm]),
+      epi(s, dslash_vals<R, DAG, MU0, UNIT>(k, pc, ld(n.tp), ld(n.tm), ld(n.xp), ld(n.xm), Wt[s], Wt[n.tm], Wx[s],
+                                            Wx[n.xm]),
           pc);
     }
   }
 }
 
-template <typename R, int DAG, bool MU0, class Epi>
+template <typename R, int DAG, bool MU0, bool UNIT = false, class Epi>
 __device__ __forceinline__ void stencil_all(const Geo& g, const OpK<R>& k, const C2<R>* __restrict__ in,
                                             const C2<R>* __restrict__ Wt, const C2<R>* __restrict__ Wx, Epi& epi) {
   auto ld = [&](int i) { return in[i]; };
-  stencil_ld<R, DAG, MU0>(g, k, ld, Wt, Wx, epi);
+  stencil_ld<R, DAG, MU0, UNIT>(g, k, ld, Wt, Wx, epi);
 }
 
 // Blocks of work of a stencil kernel (march: 8 warp items per block).
@@ -267,8 +276,8 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(Geo g, const double2* __rest
   }
 }
 
-template <typename R, bool MU0>
-__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cg1(Geo g, OpK<R> k, const C2<R>* __restrict__ r,
+template <typename R, bool MU0, bool UNIT = false>
+__global__ void __launch_bounds__(kBlock, 2) k_cg1(Geo g, OpK<R> k, const C2<R>* __restrict__ r,
                                                 const C2<R>* __restrict__ p_old, C2<R>* __restrict__ p_new,
                                                 C2<R>* __restrict__ Mp, const C2<R>* __restrict__ Wt,
                                                 const C2<R>* __restrict__ Wx, CgState* st, Red red) {
@@ -285,7 +294,7 @@ __global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cg1(Geo g, OpK<
     v = fma(o.x, o.x, v);
     v = fma(o.y, o.y, v);
   };
-  stencil_ld<R, 0, MU0>(g, k, ld, Wt, Wx, epi);
+  stencil_ld<R, 0, MU0, UNIT>(g, k, ld, Wt, Wx, epi);
   double tot;
   if (grid_sum<kBlock, R>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) {
     st->alpha = st->rr / tot;
@@ -295,19 +304,23 @@ __global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cg1(Geo g, OpK<
 }
 
 // FP64: convergence tested on the recursive residual, as hmc.c:381.
-template <bool MU0>
+// UNIT: the pair runs CG on N^dag N with N = M / m (links W / m).  Its residual
+// b - N^dag N (m^2 x) is b's residual for x, so r, p, beta and the stopping test
+// are M's, and alpha_N = m^2 alpha_M: x advances by (alpha_N / m^2) p.
+template <bool MU0, bool UNIT = false>
 __global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cg2_64(Geo g, OpK<double> k, const double2* __restrict__ Mp,
                                                    const double2* __restrict__ p, double2* __restrict__ x,
                                                    double2* __restrict__ r, const double2* __restrict__ Wt,
                                                    const double2* __restrict__ Wx, CgState* st, CgLog* log,
-                                                   Red red, Cond c) {
+                                                   Red red, Cond c, double inv_m2 = 1.0) {
   if (st->done) return;
   const double a = st->alpha;
+  const double ax = UNIT ? a * inv_m2 : a;
   double v = 0;
   auto epi = [&](int s, double2 ap, double2) {
     double2 xv = x[s], pv = p[s], rv = r[s];
-    xv.x += a * pv.x;
-    xv.y += a * pv.y;
+    xv.x += ax * pv.x;
+    xv.y += ax * pv.y;
     rv.x -= a * ap.x;
     rv.y -= a * ap.y;
     x[s] = xv;
@@ -315,7 +328,7 @@ __global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cg2_64(Geo g, O
     v = fma(rv.x, rv.x, v);
     v = fma(rv.y, rv.y, v);
   };
-  stencil_all<double, 1, MU0>(g, k, Mp, Wt, Wx, epi);
+  stencil_all<double, 1, MU0, UNIT>(g, k, Mp, Wt, Wx, epi);
   double rn;
   if (grid_sum<kBlock, double>(v, red.partials, red.counter, &rn) && threadIdx.x == 0) {
     st->iter += 1;
@@ -340,6 +353,13 @@ void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<do
   const int wk = stencil_work(g);
   const double2* p_old = w.p[half];
   double2* p_new = w.p[half ^ 1];
+  if (L.Wt1 != nullptr) {
+    TG_OP_DISPATCH(km, (k_cg1<double, MU0, true><<<occ_grid(k_cg1<double, MU0, true>, wk), kBlock, 0, s>>>(
+                            g, km, w.r, p_old, p_new, w.Mp, L.Wt1, L.Wx1, st, red)));
+    TG_OP_DISPATCH(kd, (k_cg2_64<MU0, true><<<occ_grid(k_cg2_64<MU0, true>, wk), kBlock, 0, s>>>(
+                            g, kd, w.Mp, p_new, x, w.r, L.Wt1, L.Wx1, st, log, red, c, L.inv_m2)));
+    return;
+  }
   TG_OP_DISPATCH(km, (k_cg1<double, MU0><<<occ_grid(k_cg1<double, MU0>, wk), kBlock, 0, s>>>(
                           g, km, w.r, p_old, p_new, w.Mp, L.Wt, L.Wx, st, red)));
   TG_OP_DISPATCH(kd, (k_cg2_64<MU0><<<occ_grid(k_cg2_64<MU0>, wk), kBlock, 0, s>>>(g, kd, w.Mp, p_new, x, w.r, L.Wt,
@@ -678,7 +698,7 @@ int resident_grid_nocache(const void* kernel, int work) {
 
 void link_phase_fixed(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,
                       float2* Wt32, float2* Wx32) {
-  k_link_phase<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, Wt, Wx, Wt32, Wx32);
+  k_link_phase<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, LinkOut{Wt, Wx, Wt32, Wx32});
 }
 
 void cg64_init_fixed(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,

@@ -30,14 +30,24 @@ struct Red {               // reduction scratch
 struct Links {
   const double2 *Wt, *Wx;
   const float2 *Wt32, *Wx32;
+  // W / m and 1 / m^2 for the unit-mass form of the FP64 CG (null when m = 0)
+  const double2 *Wt1 = nullptr, *Wx1 = nullptr;
+  double inv_m2 = 0;
+};
+
+// Where the link kernels write: W (FP64, FP32) and, when Wt1 is non-null, W / m
+struct LinkOut {
+  double2 *Wt, *Wx;
+  float2 *Wt32, *Wx32;
+  double2 *Wt1 = nullptr, *Wx1 = nullptr;
+  double inv_m = 0;
 };
 
 // link coefficients of A (both precisions)
-void link_phase(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, double2* Wt, double2* Wx,
-                float2* Wt32, float2* Wx32);
+void link_phase(cudaStream_t s, const Geo& g, int bc_t, int bc_x, const double2* A, const LinkOut& o);
 // A += c*mom, nadd times in sequence, then link coefficients
 void gauge_step(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double2* A, const double2* mom, double c,
-                int nadd, double2* Wt, double2* Wx, float2* Wt32, float2* Wx32);
+                int nadd, const LinkOut& o);
 // out = M in (dag = 0) or M^dag in (dag = 1); k must be the constants of that operator
 void dslash64(cudaStream_t s, const Geo& g, const OpK<double>& k, int dag, const double2* in, double2* out,
               const double2* Wt, const double2* Wx);
