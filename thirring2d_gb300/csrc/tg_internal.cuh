@@ -66,11 +66,11 @@ struct Geo {
   int mgrid;      // blocks of a column-march kernel
 };
 
-// Column march: a warp owns 32 consecutive x of one row block and walks
-// kMarchT rows in t, keeping psi(t-1), psi(t) and Wt(t-1) in registers; the
-// x neighbours come from warp shuffles (lanes 0 and 31 load the ones across
-// the warp's edge).  Per site that leaves 3 coalesced loads (psi(t+1), Wt,
-// Wx) instead of 9.
+// Column march: a warp owns 32 consecutive x and walks its range of rows in t
+// kMarchT rows at a time, keeping psi(t-1), psi(t) and Wt(t-1) in registers;
+// the x neighbours come from warp shuffles (the operands across the warp's
+// edges are fetched once per kMarchT rows by the first lanes).  Per site that
+// leaves 3 coalesced loads (psi(t+1), Wt, Wx) instead of 9.
 constexpr int kMarchT = 4;
 // Minimum resident blocks per SM the stencil kernels are compiled for.
 constexpr int kStencilBlocksPerSM = 1;  // no register cap: capping at 42 spilled heavily

@@ -1,10 +1,10 @@
 // tg_kernels.cu -- sm_103a kernels of the Thirring2D HMC hot path.
 //
 // Stencil kernels (operator applies and the CG kernels built on them) use the
-// warp column march of stencil_all(): a warp walks kMarchT rows of 32
-// consecutive x, reusing psi(t-1), psi(t), Wt(t-1) from registers and taking
-// x neighbours from warp shuffles, with the CG vector updates and norms fused
-// into the per-site epilogue.  Lattices whose nx is not a multiple of 32 (or
+// warp column march of stencil_all(): a warp walks a contiguous range of rows
+// of 32 consecutive x, reusing psi(t-1), psi(t), Wt(t-1) from registers and
+// taking x neighbours from warp shuffles, with the CG vector updates and norms
+// fused into the per-site epilogue.  Lattices whose nx is not a multiple of 32 (or
 // nt of kMarchT) use one site per thread.  Streaming kernels are one site per
 // thread over the full grid.  Reductions are deterministic (fixed shuffle
 // tree per block, partials summed in index order by the last block), so
@@ -48,49 +48,32 @@ void gauge_step(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double2* A, co
   k_gauge_step<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, A, mom, c, nadd, o);
 }
 
-// One column-march item: rows t0 .. t0+kMarchT-1 of the 32 columns
-// x = 32*xw + lane.  ld(i) yields the operand at site i (a plain load, or a
+// One warp marches rows ta .. tb-1 (tb > ta) of the 32 columns x0 = 32*xw ..
+// x0+31, lane = column.  ld(i) yields the operand at site i (a plain load, or a
 // vector recombined on the fly); epi(s, out(s), operand(s)) consumes each
-// site's result.
+// site's result.  psi(t-1), psi(t) and Wt(t-1) stay in registers from row to
+// row; x neighbours come from warp shuffles.
 template <typename R, int DAG, bool MU0, bool UNIT = false, class Ld, class Epi>
-__device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
-                                           const C2<R>* __restrict__ Wx, int item, Epi& epi) {
+__device__ __forceinline__ void march_segment(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
+                                              const C2<R>* __restrict__ Wx, int xw, int ta, int tb, Epi& epi) {
   const int nx = g.nx;
-  const int nxw = nx >> 5;
-  const int tb = item / nxw;
-  const int xw = item - tb * nxw;
-  const int t0 = tb * kMarchT;
   const int lane = threadIdx.x & 31;
   const int x0 = xw << 5;
   const int x = x0 + lane;
-  // The operands across the warp's two edges, fetched once per item by the
-  // first lanes: lane i < kMarchT the operand left of column x0 in row t0+i,
-  // lane kMarchT+i the one right of column x0+31, and lane i < kMarchT also
-  // the x link entering column x0.  Each row hands them to lanes 0 and 31 by
-  // shuffles, so no lane fetches (or recombines) an operand it does not use.
-  const int xle = (x0 == 0) ? nx - 1 : x0 - 1;
-  const int xre = (x0 + 32 == nx) ? 0 : x0 + 32;
-  C2<R> ep = mk<R>(0, 0), ew = mk<R>(0, 0);
-  if (lane < 2 * kMarchT) {
-    const int row = t0 + (lane < kMarchT ? lane : lane - kMarchT);
-    ep = ld(row * nx + (lane < kMarchT ? xle : xre));
-    if (lane < kMarchT) ew = Wx[row * nx + xle];
-  }
-  const int tm = (t0 == 0) ? g.nt - 1 : t0 - 1;
+  const int xle = (x0 == 0) ? nx - 1 : x0 - 1;       // column left of the warp
+  const int xre = (x0 + 32 == nx) ? 0 : x0 + 32;     // column right of the warp
+  const int tm = (ta == 0) ? g.nt - 1 : ta - 1;
   C2<R> pm = ld(tm * nx + x);
   C2<R> wtm = Wt[tm * nx + x];
-  C2<R> pc = ld(t0 * nx + x);
-#pragma unroll
-  for (int i = 0; i < kMarchT; i++) {
-    const int t = t0 + i;
+  C2<R> pc = ld(ta * nx + x);
+  // row t, given the operand across the warp's edge (pe: used by lanes 0 and
+  // 31) and the x link entering column x0 (we: used by lane 0)
+  auto row = [&](int t, C2<R> pe, C2<R> we) {
     const int tp = (t + 1 == g.nt) ? 0 : t + 1;
     const int s = t * nx + x;
     const C2<R> pp = ld(tp * nx + x);
     const C2<R> wt = Wt[s];
     const C2<R> wx = Wx[s];
-    const int src = (lane == 31) ? kMarchT + i : i;
-    const C2<R> pe = mk<R>(__shfl_sync(0xffffffffu, ep.x, src), __shfl_sync(0xffffffffu, ep.y, src));
-    const C2<R> we = mk<R>(__shfl_sync(0xffffffffu, ew.x, i), __shfl_sync(0xffffffffu, ew.y, i));
     C2<R> pr = shfl_down1<R>(pc);
     C2<R> pl = shfl_up1<R>(pc);
     C2<R> wl = shfl_up1<R>(wx);
@@ -103,6 +86,29 @@ __device__ __forceinline__ void march_item(const Geo& g, const OpK<R>& k, Ld& ld
     pm = pc;
     pc = pp;
     wtm = wt;
+  };
+  int t = ta;
+  for (; t + kMarchT <= tb; t += kMarchT) {
+    // The edge operands of kMarchT rows, fetched once by the first lanes: lane
+    // i < kMarchT the operand left of x0 in row t+i (and the x link entering
+    // x0), lane kMarchT+i the operand right of x0+31.  Shuffles hand them to
+    // lanes 0 and 31, so no lane fetches or recombines an operand it does not use.
+    C2<R> ep = mk<R>(0, 0), ew = mk<R>(0, 0);
+    if (lane < 2 * kMarchT) {
+      const int rr = t + (lane < kMarchT ? lane : lane - kMarchT);
+      ep = ld(rr * nx + (lane < kMarchT ? xle : xre));
+      if (lane < kMarchT) ew = Wx[rr * nx + xle];
+    }
+#pragma unroll
+    for (int i = 0; i < kMarchT; i++) {
+      const int src = (lane == 31) ? kMarchT + i : i;
+      row(t + i, mk<R>(__shfl_sync(0xffffffffu, ep.x, src), __shfl_sync(0xffffffffu, ep.y, src)),
+          mk<R>(__shfl_sync(0xffffffffu, ew.x, i), __shfl_sync(0xffffffffu, ew.y, i)));
+    }
+  }
+  for (; t < tb; t++) {  // the last rows of the segment: lanes 0 and 31 fetch their own
+    const int xe = (lane == 31) ? xre : xle;
+    row(t, ld(t * nx + xe), Wx[t * nx + xle]);
   }
 }
 
@@ -112,10 +118,22 @@ template <typename R, int DAG, bool MU0, bool UNIT = false, class Ld, class Epi>
 __device__ __forceinline__ void stencil_ld(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
                                            const C2<R>* __restrict__ Wx, Epi& epi) {
   if (g.march) {
-    const int items = (g.nx >> 5) * (g.nt / kMarchT);
+    // The (strip, t) rows of the lattice in strip-major order, split into
+    // one contiguous range per warp: ranges differ by at most one row, and a
+    // warp restarts its march only where its range crosses into a new strip.
     constexpr int wpb = kBlock / 32;
-    for (int item = blockIdx.x * wpb + (threadIdx.x >> 5); item < items; item += gridDim.x * wpb)
-      march_item<R, DAG, MU0, UNIT>(g, k, ld, Wt, Wx, item, epi);
+    const long long rows = (long long)(g.nx >> 5) * g.nt;
+    const long long nw = (long long)gridDim.x * wpb;
+    const long long gw = (long long)blockIdx.x * wpb + (threadIdx.x >> 5);
+    long long r = rows * gw / nw;
+    const long long r1 = rows * (gw + 1) / nw;
+    while (r < r1) {
+      const int xw = (int)(r / g.nt);
+      const int ta = (int)(r - (long long)xw * g.nt);
+      const int tb = (r1 - r < (long long)(g.nt - ta)) ? ta + (int)(r1 - r) : g.nt;
+      march_segment<R, DAG, MU0, UNIT>(g, k, ld, Wt, Wx, xw, ta, tb, epi);
+      r += tb - ta;
+    }
   } else {
     TG_SITES(s, g.V) {
       int t, x;
@@ -136,9 +154,9 @@ __device__ __forceinline__ void stencil_all(const Geo& g, const OpK<R>& k, const
   stencil_ld<R, DAG, MU0, UNIT>(g, k, ld, Wt, Wx, epi);
 }
 
-// Blocks of work of a stencil kernel (march: 8 warp items per block).
+// Blocks of work of a stencil kernel (march: at least kMarchT rows per warp).
 inline int stencil_work(const Geo& g) {
-  return g.march ? ((g.nx >> 5) * (g.nt / kMarchT) + kBlock / 32 - 1) / (kBlock / 32) : nblocks(g.V);
+  return g.march ? ((g.nx >> 5) * ((g.nt + kMarchT - 1) / kMarchT) + kBlock / 32 - 1) / (kBlock / 32) : nblocks(g.V);
 }
 
 // Grid = resident blocks of this kernel on the GPU (one wave), at most `work`.
@@ -308,7 +326,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg1(Geo g, OpK<R> k, const C2<R>*
 // b - N^dag N (m^2 x) is b's residual for x, so r, p, beta and the stopping test
 // are M's, and alpha_N = m^2 alpha_M: x advances by (alpha_N / m^2) p.
 template <bool MU0, bool UNIT = false>
-__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cg2_64(Geo g, OpK<double> k, const double2* __restrict__ Mp,
+__global__ void __launch_bounds__(kBlock, 2) k_cg2_64(Geo g, OpK<double> k, const double2* __restrict__ Mp,
                                                    const double2* __restrict__ p, double2* __restrict__ x,
                                                    double2* __restrict__ r, const double2* __restrict__ Wt,
                                                    const double2* __restrict__ Wx, CgState* st, CgLog* log,
