@@ -36,6 +36,7 @@ extern "C" {
 #define TG_E_CUDA 4     /* CUDA runtime error                                                 */
 #define TG_E_ARG 5      /* invalid argument                                                   */
 #define TG_E_ALLOC 6    /* device or pinned allocation failed                                 */
+#define TG_E_TIMEOUT 7  /* a grid barrier of the persistent solver waited past its limit      */
 
 /* ---- boundary conditions (sign of the hop across the last slice) ------- */
 #define TG_BC_PERIODIC 1
@@ -66,8 +67,14 @@ typedef struct {
   int maxiter;      /* iteration cap (hmc.c:35 CG_MAX_ITER = 100000)                  */
   int precision;    /* TG_PREC_*                                                      */
   int ru_interval;  /* TG_PREC_MIXED: FP32 iterations between FP64 reliable updates   */
-  int pad_;
+  int solver;       /* TG_SOLVER_*: how the iterations are scheduled (0 = default)    */
 } tg_cg_params;
+
+/* tg_cg_params.solver.  Both run the same iteration and stopping rules; they
+ * differ in rounding of the grid sums only. */
+#define TG_SOLVER_DEFAULT 0     /* the faster of the two on this library's measurements       */
+#define TG_SOLVER_LAUNCHES 1    /* two kernel launches per iteration (graph WHILE node)       */
+#define TG_SOLVER_PERSISTENT 2  /* one cooperative launch per solve, grid barriers inside     */
 
 typedef struct {
   int iterations;       /* CG iterations (each = one M and one M^dagger apply) */

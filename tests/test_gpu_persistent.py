@@ -1,0 +1,132 @@
+"""The persistent CG solver (TG_SOLVER_PERSISTENT: one cooperative launch per
+solve, grid barriers inside) against the reference's outputs, the oracle and
+the launch-per-iteration solver: same stopping rules (hmc.c:341-404), same
+solutions to rounding, same trajectories."""
+import numpy as np
+import pytest
+
+from helpers import STABLE, TRAJ_CONFIGS, dH_ok, golden, lat_args, rel
+
+pytestmark = pytest.mark.gpu
+
+PERSISTENT = 2
+LAUNCHES = 1
+
+
+@pytest.fixture(scope="module")
+def tg():
+    import thirring2d_gb300 as tg
+    tg.native.load()
+    return tg
+
+
+def make(tg, d):
+    return tg.Lattice(*lat_args(d))
+
+
+def cplx(rng, shape):
+    return rng.normal(size=shape) + 1j * rng.normal(size=shape)
+
+
+@pytest.mark.parametrize("name", TRAJ_CONFIGS)
+def test_persistent_cg_golden(tg, name):
+    d = golden(name)
+    L = make(tg, d)
+    L.set_gauge(d["A"])
+    x, res = L.fmdm_invert_cg(d["psi"], tg.cg_params(solver=PERSISTENT))  # hmc.c's stop |r|^2 < 1e-30
+    assert res.status == 0
+    assert rel(x, d["cg_x"]) < 1e-12
+
+
+@pytest.mark.parametrize("nt,nx,mu", [(64, 64, 0.0), (96, 128, 0.3), (12, 10, 0.0), (2, 64, 0.0)])
+def test_persistent_equals_launches(tg, oracle_lib, nt, nx, mu):
+    rng = np.random.default_rng(nt * 1000 + nx)
+    A = rng.normal(0, 0.5, (nt, nx, 2))
+    b = cplx(rng, (nt, nx))
+    L = tg.Lattice(nt, nx, 0.2, 0.5, mu, -1, 1)
+    L.set_gauge(A)
+    out = {}
+    for solver in (LAUNCHES, PERSISTENT):
+        out[solver] = L.fmdm_invert_cg(b, tg.cg_params(rel_tol=1e-12, abs_tol2=0, solver=solver))
+    (x1, r1), (x2, r2) = out[LAUNCHES], out[PERSISTENT]
+    assert r1.status == r2.status == 0
+    assert abs(r1.iterations - r2.iterations) <= 2
+    assert rel(x2, x1) < 1e-11
+    # the stop tests the recursive residual (1e-12); the true one drifts above it
+    # by the same amount in both solvers
+    o = oracle_lib.Oracle(nt, nx, 0.2, 0.5, mu, -1, 1)
+    true = [np.linalg.norm(b - o.Mdag(A, o.M(A, x))) / np.linalg.norm(b) for x in (x1, x2)]
+    assert true[1] < 5e-11 and true[1] < 3 * true[0] + 1e-12, true
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_persistent_1024(tg, oracle_lib, precision):
+    """The 1024^2 workload: true residual below the target, iteration counts
+    as the launch-per-iteration solver's."""
+    n = 1024
+    rng = np.random.default_rng(1024)
+    A = rng.normal(0, 0.3, (n, n, 2))
+    b = cplx(rng, (n, n))
+    L = tg.Lattice(n, n, 0.05, 0.6, 0.0, -1, 1)
+    L.set_gauge(A)
+    cp = dict(rel_tol=1e-10, abs_tol2=0, precision=precision, ru_interval=50)
+    x, res = L.fmdm_invert_cg(b, tg.cg_params(solver=PERSISTENT, **cp))
+    _, ref = L.fmdm_invert_cg(b, tg.cg_params(solver=LAUNCHES, **cp))
+    assert res.status == 0
+    assert abs(res.iterations - ref.iterations) <= max(3, ref.iterations // 50)
+    o = oracle_lib.Oracle(n, n, 0.05, 0.6, 0.0, -1, 1)
+    r = b - o.Mdag(A, o.M(A, x))
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1.5e-10
+    if precision == 1:
+        assert res.reliable_updates >= 1
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_persistent_edge_cases(tg, precision):
+    rng = np.random.default_rng(9)
+    L = tg.Lattice(32, 32, 0.3, 0.5, 0.0, -1, 1)
+    L.set_gauge(rng.normal(0, 0.5, (32, 32, 2)))
+    cp = dict(solver=PERSISTENT, precision=precision, ru_interval=50)
+    x, res = L.fmdm_invert_cg(np.zeros((32, 32), complex), tg.cg_params(**cp))  # hmc.c:359-361
+    assert res.status == 0 and res.iterations == 0 and not x.any()
+    x, res = L.fmdm_invert_cg(cplx(rng, (32, 32)), tg.cg_params(maxiter=3, **cp))
+    assert res.status == tg.native.TG_E_NOCONV and res.iterations == 3
+    bad = cplx(rng, (32, 32))
+    bad[2, 3] = np.nan
+    x, res = L.fmdm_invert_cg(bad, tg.cg_params(**cp))
+    assert res.status == tg.native.TG_E_NAN
+    # the lattice is still usable afterwards
+    x, res = L.fmdm_invert_cg(cplx(rng, (32, 32)), tg.cg_params(rel_tol=1e-10, abs_tol2=0, **cp))
+    assert res.status == 0
+
+
+def _replay(tg, d, hp):
+    L = make(tg, d)
+    L.seed_mersenne(int(d["traj_seed"]), 543210)
+    L.update_puregauge_hb(int(d["traj_sweeps"]))
+    return L, [L.update_gauge(hp) for _ in range(len(d["traj_stats"]))]
+
+
+@pytest.mark.parametrize("name", TRAJ_CONFIGS)
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_persistent_trajectories_golden(tg, name, use_graph):
+    d = golden(name)
+    hp = tg.hmc_params(nsteps=int(d["traj_nsteps"]), tau=1.0, npf=1, stochastic_term=True,
+                       rng=tg.native.RNG_MT, use_graph=use_graph, cg=tg.cg_params(solver=PERSISTENT))
+    L, res = _replay(tg, d, hp)
+    for k, (r, want) in enumerate(zip(res, d["traj_stats"])):
+        assert r.status == 0
+        assert dH_ok(r.dH, want[0], name in STABLE), (k, r.dH, want[0])
+        assert r.accepted == int(want[9])
+    assert np.abs(L.get_gauge() - d["traj_A"][-1]).max() < 1e-9
+
+
+def test_persistent_mixed_trajectory(tg):
+    d = golden("c1s_16x16_px")
+    hp = tg.hmc_params(nsteps=40, rng=tg.native.RNG_MT,
+                       cg=tg.cg_params(rel_tol=1e-12, abs_tol2=0, precision=1, ru_interval=50, solver=PERSISTENT))
+    _, res = _replay(tg, d, hp)
+    for r, want in zip(res, d["traj_stats"]):
+        assert abs(r.dH - want[0]) < 1e-9
+        assert r.accepted == int(want[9])
+        assert r.reliable_updates > 0

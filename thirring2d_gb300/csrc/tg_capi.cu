@@ -121,6 +121,8 @@ struct tg_lattice {
   CgLog* log = nullptr;
   TrajStats* ts = nullptr;
   Red red{};
+  unsigned* bar = nullptr;      // persistent solver: grid barrier {count, gen}
+  double* pcg_part = nullptr;   // and its partial sums [2 * kPcgMaxGrid]
 
   double* h_stage = nullptr;  // pinned, 2*V*kMaxPf doubles... sized at create
   size_t h_stage_len = 0;
@@ -151,6 +153,9 @@ OpK<float> op_k32(const tg_lattice* L, int dagger) {
   f.m = (float)k.m; f.cf = (float)k.cf; f.cb = (float)k.cb; f.mu0 = k.mu0;
   return f;
 }
+// TG_SOLVER_DEFAULT: launch-per-iteration kernels unless measured otherwise
+constexpr bool kDefaultPersistent = false;
+
 // The FP64 CG runs in unit-mass form (links W / m) whenever 1/m is a finite
 // nonzero number; m = 0 keeps the plain form.
 bool unit_mass(const tg_lattice* L) {
@@ -219,6 +224,7 @@ int check_cg_params(const tg_cg_params* cp) {
   if (cp->maxiter <= 0) return fail(TG_E_ARG, "maxiter must be positive");
   if (cp->precision != TG_PREC_FP64 && cp->precision != TG_PREC_MIXED) return fail(TG_E_ARG, "bad precision");
   if (cp->precision == TG_PREC_MIXED && cp->ru_interval <= 0) return fail(TG_E_ARG, "ru_interval must be positive");
+  if (cp->solver < TG_SOLVER_DEFAULT || cp->solver > TG_SOLVER_PERSISTENT) return fail(TG_E_ARG, "bad solver");
   if (!(cp->rel_tol >= 0) || !(cp->abs_tol2 >= 0)) return fail(TG_E_ARG, "tolerances must be >= 0");
   return TG_OK;
 }
@@ -257,8 +263,83 @@ int capture_graph_of(cudaStream_t s, cudaGraph_t* gr) {
 // capturing and the iteration loop becomes a conditional WHILE node (no host
 // involvement at run time).  graph = false: iterations are launched in
 // chunks and the host polls the device `done` flag between chunks.
+bool use_persistent(const tg_cg_params& cp) {
+  if (cp.solver == TG_SOLVER_PERSISTENT) return true;
+  if (cp.solver == TG_SOLVER_LAUNCHES) return false;
+  const char* e = getenv("TG_SOLVER");  // default: TG_SOLVER=persistent|launches overrides
+  if (e && strcmp(e, "persistent") == 0) return true;
+  if (e && strcmp(e, "launches") == 0) return false;
+  return kDefaultPersistent;
+}
+
+// The whole solve as one cooperative launch (tg_pcg.cu); the barrier's
+// arrival count is cleared first, so a solve that timed out leaves no trace.
+int enqueue_pcg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const double2* b, double2* x, int log_index) {
+  const Links lk = links(L);
+  const GridBar bar{L->bar, L->bar + 1};
+  TG_CK(cudaMemsetAsync(L->bar, 0, sizeof(unsigned), s));
+  cudaError_t e;
+  if (cp.precision == TG_PREC_MIXED) {
+    PcgMxArgs a{};
+    a.g = L->g;
+    a.km32 = op_k32(L, 0);
+    a.kd32 = op_k32(L, 1);
+    a.km = op_k(L, 0);
+    a.kd = op_k(L, 1);
+    a.Wt32 = lk.Wt32;
+    a.Wx32 = lk.Wx32;
+    a.Wt = lk.Wt;
+    a.Wx = lk.Wx;
+    a.b = b;
+    a.x = x;
+    a.tmp = L->wmx.tmp64;
+    a.xs = L->wmx.xs;
+    a.r = L->wmx.rs;
+    a.p0 = L->wmx.ps[0];
+    a.p1 = L->wmx.ps[1];
+    a.Mp = L->wmx.Mps;
+    a.st = L->st;
+    a.log = L->log;
+    a.log_index = log_index;
+    a.part = L->pcg_part;
+    a.bar = bar;
+    a.rel_tol = cp.rel_tol;
+    a.abs_tol2 = cp.abs_tol2;
+    a.maxiter = cp.maxiter;
+    a.ru_interval = cp.ru_interval;
+    e = pcgmx(s, L->P.mu == 0.0, a);
+  } else {
+    Pcg64Args a{};
+    a.g = L->g;
+    a.km = op_k(L, 0);
+    a.kd = op_k(L, 1);
+    const bool unit = lk.Wt1 != nullptr;
+    a.Wt = unit ? lk.Wt1 : lk.Wt;
+    a.Wx = unit ? lk.Wx1 : lk.Wx;
+    a.inv_m2 = unit ? lk.inv_m2 : 0.0;
+    a.b = b;
+    a.x = x;
+    a.r = L->w64.r;
+    a.p0 = L->w64.p[0];
+    a.p1 = L->w64.p[1];
+    a.Mp = L->w64.Mp;
+    a.st = L->st;
+    a.log = L->log;
+    a.log_index = log_index;
+    a.part = L->pcg_part;
+    a.bar = bar;
+    a.rel_tol = cp.rel_tol;
+    a.abs_tol2 = cp.abs_tol2;
+    a.maxiter = cp.maxiter;
+    e = pcg64(s, L->P.mu == 0.0, a);
+  }
+  if (e != cudaSuccess) return fail(TG_E_CUDA, std::string("persistent CG launch: ") + cudaGetErrorString(e));
+  return TG_OK;
+}
+
 int enqueue_cg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const double2* b, double2* x, int log_index,
                bool graph) {
+  if (use_persistent(cp)) return enqueue_pcg(L, s, cp, b, x, log_index);
   const Geo& g = L->g;
   const bool mixed = cp.precision == TG_PREC_MIXED;
   OpK<double> km = op_k(L, 0), kd = op_k(L, 1);
@@ -358,8 +439,8 @@ template <typename F> int run_maybe_graph(tg_lattice* L, const std::string& key,
 
 std::string cg_key(const tg_cg_params& cp) {
   char buf[160];
-  snprintf(buf, sizeof buf, "%.17g/%.17g/%d/%d/%d", cp.rel_tol, cp.abs_tol2, cp.maxiter, cp.precision,
-           cp.ru_interval);
+  snprintf(buf, sizeof buf, "%.17g/%.17g/%d/%d/%d/%d", cp.rel_tol, cp.abs_tol2, cp.maxiter, cp.precision,
+           cp.ru_interval, use_persistent(cp) ? 1 : 0);
   return buf;
 }
 
@@ -394,6 +475,7 @@ int solver_status(int status) {
     case TG_E_NOCONV: return fail(TG_E_NOCONV, "CG reached its iteration cap");
     case TG_E_DIVERGED: return fail(TG_E_DIVERGED, "Cannot invert fermion matrix (|r|^2/|r0|^2 > 1e10)");
     case TG_E_NAN: return fail(TG_E_NAN, "NaN in the CG recurrence");
+    case TG_E_TIMEOUT: return fail(TG_E_TIMEOUT, "persistent CG: a grid barrier waited past its limit");
     default: return fail(status, "solver error");
   }
 }
@@ -639,7 +721,8 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
     if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
   if ((rc = dmalloc(&L->st, 1)) != TG_OK || (rc = dmalloc(&L->log, kMaxLog)) != TG_OK ||
       (rc = dmalloc(&L->ts, 1)) != TG_OK || (rc = dmalloc(&L->red.partials, (size_t)nblocks((int)V) + 32)) != TG_OK ||
-      (rc = dmalloc(&L->red.counter, 1)) != TG_OK)
+      (rc = dmalloc(&L->red.counter, 1)) != TG_OK || (rc = dmalloc(&L->bar, 2)) != TG_OK ||
+      (rc = dmalloc(&L->pcg_part, 2 * (size_t)kPcgMaxGrid)) != TG_OK)
     return bail(rc);
   if ((rc = ensure_pf(L, 1)) != TG_OK) return bail(rc);
   L->h_stage_len = (size_t)(kMaxPf + 2) * 2 * n;  // npf eta fields + momenta + noise
@@ -651,6 +734,7 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
   if (cudaMemsetAsync(L->A, 0, n * sizeof(double2), L->stream) != cudaSuccess ||
       cudaMemsetAsync(L->noise, 0, n * sizeof(double2), L->stream) != cudaSuccess ||
       cudaMemsetAsync(L->red.counter, 0, sizeof(unsigned), L->stream) != cudaSuccess ||
+      cudaMemsetAsync(L->bar, 0, 2 * sizeof(unsigned), L->stream) != cudaSuccess ||
       cudaMemsetAsync(L->ts, 0, sizeof(TrajStats), L->stream) != cudaSuccess ||
       cudaMemsetAsync(L->st, 0, sizeof(CgState), L->stream) != cudaSuccess)
     return bail(fail(TG_E_CUDA, "initial memset failed"));
@@ -674,7 +758,7 @@ int tg_destroy(tg_lattice* L) {
   void* dev[] = {L->A, L->Anew, L->Wt, L->Wx, L->Wt1, L->Wx1, L->mom, L->noise, L->chi, L->Mchi, L->vin, L->vout, L->w64.r,
                  L->w64.p[0], L->w64.p[1], L->w64.Mp, L->wmx.tmp64, L->Wt32, L->Wx32, L->wmx.xs, L->wmx.rs,
                  L->wmx.ps[0], L->wmx.ps[1], L->wmx.Mps,
-                 L->st, L->log, L->ts, L->red.partials, L->red.counter, L->eta, L->phi, L->unif, L->mask,
+                 L->st, L->log, L->ts, L->red.partials, L->red.counter, L->bar, L->pcg_part, L->eta, L->phi, L->unif, L->mask,
                  L->rv[0], L->rv[1], L->rv[2], L->rv[3], L->rv[4], L->rv[5]};
   for (void* d : dev)
     if (d) cudaFree(d);

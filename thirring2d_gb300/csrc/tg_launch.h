@@ -111,6 +111,52 @@ void dense_M(cudaStream_t s, const Geo& g, const OpK<double>& k, const double2* 
 // log|det| and arg det of nmat V x V complex matrices (overwritten by their LU factors)
 void lu_logdet(cudaStream_t s, int V, int nmat, double2* mats, double* out);
 
+// ---------------------------------------------------------------------------
+// Persistent CG (tg_pcg.cu): one cooperative launch per solve
+// ---------------------------------------------------------------------------
+struct GridBar {       // grid barrier: arrivals and generation (count must be 0 at launch)
+  unsigned* count;
+  unsigned* gen;
+};
+constexpr int kPcgMaxGrid = 4096;  // partial sums: 2 * kPcgMaxGrid doubles
+
+struct Pcg64Args {
+  Geo g;
+  OpK<double> km, kd;
+  const double2 *Wt, *Wx;  // W, or W / m with inv_m2 = 1 / m^2 (unit-mass form); inv_m2 = 0: plain
+  double inv_m2;
+  const double2* b;
+  double2 *x, *r, *p0, *p1, *Mp;
+  CgState* st;
+  CgLog* log;
+  int log_index;
+  double* part;
+  GridBar bar;
+  double rel_tol, abs_tol2;
+  int maxiter;
+};
+
+struct PcgMxArgs {
+  Geo g;
+  OpK<float> km32, kd32;
+  OpK<double> km, kd;
+  const float2 *Wt32, *Wx32;
+  const double2 *Wt, *Wx;
+  const double2* b;
+  double2 *x, *tmp;
+  float2 *xs, *r, *p0, *p1, *Mp;
+  CgState* st;
+  CgLog* log;
+  int log_index;
+  double* part;
+  GridBar bar;
+  double rel_tol, abs_tol2;
+  int maxiter, ru_interval;
+};
+
+cudaError_t pcg64(cudaStream_t s, bool mu0, Pcg64Args a);
+cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a);
+
 // FP64 FMA throughput probe: grid * 256 * 32 * iters FMAs, writes nothing
 void dfma_peak(cudaStream_t s, int grid, int iters, double* sink);
 

@@ -1,0 +1,370 @@
+// tg_pcg.cu -- the persistent CG solver: one cooperative launch runs a whole
+// solve of M^dag M x = b (fmdm_invert_cg, hmc.c:341-404), FP64 or FP32 with
+// FP64 reliable updates, instead of two launches per iteration.
+//
+// All blocks are co-resident (cooperative launch) and meet at a grid barrier
+// after each reduction.  Every block writes its partial sum, passes the
+// barrier, and then adds all partials in index order itself, so every block
+// holds the same bitwise total and takes the same branch: control flow stays
+// uniform across the grid without a broadcast.  Two partial arrays alternate,
+// so a block that races ahead never overwrites partials another block is
+// still reading.  Vectors that other blocks write during the solve are read
+// with ld.global.cg (L2), so no SM sees a stale L1 line.  Each block marches
+// the same row ranges in every phase (tg_stencil.cuh).
+//
+// The barrier's wait is bounded: after kBarrierSpinLimit polls a block gives
+// up, the solve ends with TG_E_TIMEOUT, and every other block times out at
+// its next barrier, so a fault in the scheme cannot hang the GPU.
+#include <math.h>
+
+#include <mutex>
+#include <unordered_map>
+
+#include "tg_stencil.cuh"
+
+namespace tg {
+
+constexpr long long kBarrierSpinLimit = 1LL << 24;  // polls of >= 64 ns: over a second
+
+__device__ __forceinline__ bool grid_barrier(const GridBar& b) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = b.gen;
+    const unsigned gen = *vgen;  // read before arriving: the last arrival bumps it
+    __threadfence();
+    const unsigned arrived = atomicAdd(b.count, 1u);
+    int ok = 1;
+    if (arrived == gridDim.x - 1) {
+      atomicExch(b.count, 0u);
+      __threadfence();
+      atomicAdd(b.gen, 1u);
+    } else {
+      long long spins = 0;
+      while (*vgen == gen) {
+        if (++spins > kBarrierSpinLimit) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Grid total of v, the same value in every thread of every block.
+__device__ __forceinline__ bool grid_total(double v, double* part, const GridBar& bar, double& out) {
+  __shared__ double sh[kBlock / 32];
+  __shared__ double s_tot;
+  const double b = block_sum<kBlock, double>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
+  if (!grid_barrier(bar)) return false;
+  double s = 0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += kBlock) s += __ldcg(part + i);
+  s = block_sum<kBlock, double>(s, sh);
+  if (threadIdx.x == 0) s_tot = s;
+  __syncthreads();
+  out = s_tot;
+  return true;
+}
+
+__device__ __forceinline__ void pcg_report(CgState* st, CgLog* log, int log_index, double rr, double rr0, double stop,
+                                           int iter, int n_ru, int status) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  st->rr = rr;
+  st->rr0 = rr0;
+  st->rr_true = rr;
+  st->stop = stop;
+  st->iter = iter;
+  st->n_ru = n_ru;
+  st->status = status;
+  st->done = 1;
+  st->need_ru = 0;
+  st->restart = 0;
+  st->log_index = log_index;
+  if (log != nullptr && log_index >= 0) {
+    CgLog& l = log[log_index];
+    l.iter = iter;
+    l.status = status;
+    l.n_ru = n_ru;
+    l.rr = rr;
+    l.rr0 = rr0;
+  }
+}
+
+__device__ __forceinline__ double stop_of(double rr0, double rel_tol, double abs_tol2) {
+  double stop = abs_tol2;
+  if (rel_tol > 0 && rel_tol * rel_tol * rr0 > stop) stop = rel_tol * rel_tol * rr0;
+  return stop;
+}
+
+// ---------------------------------------------------------------------------
+// FP64: the iteration of k_cg1 + k_cg2_64 (unit-mass form when UNIT)
+// ---------------------------------------------------------------------------
+template <bool MU0, bool UNIT>
+__global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
+  const Geo& g = a.g;
+  double* partA = a.part;
+  double* partB = a.part + gridDim.x;
+  double v = 0;
+  TG_SITES(s, g.V) {  // x = 0, r = p = b (hmc.c:352-357)
+    const double2 bb = a.b[s];
+    a.x[s] = make_double2(0.0, 0.0);
+    a.r[s] = bb;
+    a.p0[s] = bb;
+    v = fma(bb.x, bb.x, v);
+    v = fma(bb.y, bb.y, v);
+  }
+  double rr = 0;
+  int status = -1, iter = 0;
+  if (!grid_total(v, partB, a.bar, rr)) status = TG_E_TIMEOUT;
+  const double rr0 = rr;
+  const double stop = stop_of(rr0, a.rel_tol, a.abs_tol2);
+  if (status < 0) {
+    if (isnan(rr)) status = TG_E_NAN;
+    else if (!(rr >= stop) || rr == 0.0) status = TG_OK;  // hmc.c:359-361
+  }
+  double beta = 0;
+  int half = 0;
+  while (status < 0) {
+    const double2* p_old = half ? a.p1 : a.p0;
+    double2* p_new = half ? a.p0 : a.p1;
+    double va = 0;
+    auto ld_a = [&](int i) {
+      const double2 rv = __ldcg(a.r + i), pv = __ldcg(p_old + i);
+      return make_double2(fma(beta, pv.x, rv.x), fma(beta, pv.y, rv.y));
+    };
+    auto epi_a = [&](int s, double2 o, double2 pc) {
+      p_new[s] = pc;
+      a.Mp[s] = o;
+      va = fma(o.x, o.x, va);
+      va = fma(o.y, o.y, va);
+    };
+    stencil_ld<double, 0, MU0, UNIT>(g, a.km, ld_a, a.Wt, a.Wx, epi_a);
+    double pap;
+    if (!grid_total(va, partA, a.bar, pap)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    const double alpha = rr / pap;
+    const double ax = UNIT ? alpha * a.inv_m2 : alpha;
+    double vb = 0;
+    auto ld_b = [&](int i) { return __ldcg(a.Mp + i); };
+    auto epi_b = [&](int s, double2 ap, double2) {
+      double2 xv = __ldcg(a.x + s), pv = __ldcg(p_new + s), rv = __ldcg(a.r + s);
+      xv.x += ax * pv.x;
+      xv.y += ax * pv.y;
+      rv.x -= alpha * ap.x;
+      rv.y -= alpha * ap.y;
+      a.x[s] = xv;
+      a.r[s] = rv;
+      vb = fma(rv.x, rv.x, vb);
+      vb = fma(rv.y, rv.y, vb);
+    };
+    stencil_ld<double, 1, MU0, UNIT>(g, a.kd, ld_b, a.Wt, a.Wx, epi_b);
+    double rn;
+    if (!grid_total(vb, partB, a.bar, rn)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    iter += 1;
+    beta = rn / rr;
+    rr = rn;
+    if (isnan(rn)) status = TG_E_NAN;
+    else if (rn < stop) status = TG_OK;                   // hmc.c:381
+    else if (rn / rr0 > 1e10) status = TG_E_DIVERGED;     // hmc.c:383-386
+    else if (iter >= a.maxiter) status = TG_E_NOCONV;
+    half ^= 1;
+  }
+  pcg_report(a.st, a.log, a.log_index, rr, rr0, stop, iter, 0, status);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed: the iteration of k_cg1<float> + k_cgmx2, and the reliable update of
+// k_ru1..3 with the same triggers and restart rule.
+// ---------------------------------------------------------------------------
+template <bool MU0>
+__global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
+  const Geo& g = a.g;
+  double* partA = a.part;
+  double* partB = a.part + gridDim.x;
+  double v = 0;
+  TG_SITES(s, g.V) {
+    const double2 bb = a.b[s];
+    a.x[s] = make_double2(0.0, 0.0);
+    const float2 rb = make_float2((float)bb.x, (float)bb.y);
+    a.r[s] = rb;
+    a.p0[s] = rb;
+    a.xs[s] = make_float2(0.f, 0.f);
+    v = fma(bb.x, bb.x, v);
+    v = fma(bb.y, bb.y, v);
+  }
+  double rr = 0;
+  int status = -1, iter = 0, n_ru = 0, since_ru = 0;
+  if (!grid_total(v, partB, a.bar, rr)) status = TG_E_TIMEOUT;
+  const double rr0 = rr;
+  const double stop = stop_of(rr0, a.rel_tol, a.abs_tol2);
+  double rr_true = rr;
+  if (status < 0) {
+    if (isnan(rr)) status = TG_E_NAN;
+    else if (!(rr >= stop) || rr == 0.0) status = TG_OK;
+  }
+  double beta = 0;
+  int half = 0;
+  while (status < 0) {
+    const float2* p_old = half ? a.p1 : a.p0;
+    float2* p_new = half ? a.p0 : a.p1;
+    const float bf = (float)beta;
+    float va = 0;
+    auto ld_a = [&](int i) {
+      const float2 rv = __ldcg(a.r + i), pv = __ldcg(p_old + i);
+      return make_float2(fmaf(bf, pv.x, rv.x), fmaf(bf, pv.y, rv.y));
+    };
+    auto epi_a = [&](int s, float2 o, float2 pc) {
+      p_new[s] = pc;
+      a.Mp[s] = o;
+      va = fmaf(o.x, o.x, va);
+      va = fmaf(o.y, o.y, va);
+    };
+    stencil_ld<float, 0, MU0>(g, a.km32, ld_a, a.Wt32, a.Wx32, epi_a);
+    double pap;
+    if (!grid_total((double)va, partA, a.bar, pap)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    const float af = (float)(rr / pap);
+    float vb = 0;
+    auto ld_b = [&](int i) { return __ldcg(a.Mp + i); };
+    auto epi_b = [&](int s, float2 ap, float2) {
+      float2 xv = __ldcg(a.xs + s), pv = __ldcg(p_new + s), rv = __ldcg(a.r + s);
+      xv.x = fmaf(af, pv.x, xv.x);
+      xv.y = fmaf(af, pv.y, xv.y);
+      rv.x = fmaf(-af, ap.x, rv.x);
+      rv.y = fmaf(-af, ap.y, rv.y);
+      a.xs[s] = xv;
+      a.r[s] = rv;
+      vb = fmaf(rv.x, rv.x, vb);
+      vb = fmaf(rv.y, rv.y, vb);
+    };
+    stencil_ld<float, 1, MU0>(g, a.kd32, ld_b, a.Wt32, a.Wx32, epi_b);
+    double rn;
+    if (!grid_total((double)vb, partB, a.bar, rn)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    iter += 1;
+    since_ru += 1;
+    beta = rn / rr;
+    rr = rn;
+    half ^= 1;
+    const bool need = since_ru >= a.ru_interval || rn < stop || rn < kRuDrop * rr_true || iter >= a.maxiter ||
+                      rn / rr0 > 1e10 || isnan(rn);
+    if (!need) continue;
+    // reliable update: x += xs, xs = 0; r = b - M^dag M x in FP64; rs = (float) r
+    TG_SITES(s, g.V) {
+      const float2 d = __ldcg(a.xs + s);
+      double2 xv = __ldcg(a.x + s);
+      xv.x += (double)d.x;
+      xv.y += (double)d.y;
+      a.x[s] = xv;
+      a.xs[s] = make_float2(0.f, 0.f);
+    }
+    if (!grid_barrier(a.bar)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    auto ld_x = [&](int i) { return __ldcg(a.x + i); };
+    auto epi_x = [&](int s, double2 o, double2) { a.tmp[s] = o; };
+    stencil_ld<double, 0, MU0>(g, a.km, ld_x, a.Wt, a.Wx, epi_x);
+    if (!grid_barrier(a.bar)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    double vt = 0;
+    auto ld_t = [&](int i) { return __ldcg(a.tmp + i); };
+    auto epi_t = [&](int s, double2 ap, double2) {
+      const double2 bb = a.b[s];
+      const double2 rv = make_double2(bb.x - ap.x, bb.y - ap.y);
+      a.r[s] = make_float2((float)rv.x, (float)rv.y);
+      vt = fma(rv.x, rv.x, vt);
+      vt = fma(rv.y, rv.y, vt);
+    };
+    stencil_ld<double, 1, MU0>(g, a.kd, ld_t, a.Wt, a.Wx, epi_t);
+    double rt;
+    if (!grid_total(vt, partA, a.bar, rt)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    if (rt > kRuRestart * rr) beta = 0;  // the recursive residual was far too optimistic: restart p from r
+    rr_true = rt;
+    rr = rt;
+    since_ru = 0;
+    n_ru += 1;
+    if (isnan(rt)) status = TG_E_NAN;
+    else if (rt < stop) status = TG_OK;
+    else if (rt / rr0 > 1e10) status = TG_E_DIVERGED;
+    else if (iter >= a.maxiter) status = TG_E_NOCONV;
+  }
+  pcg_report(a.st, a.log, a.log_index, rr, rr0, stop, iter, n_ru, status);
+}
+
+// ---------------------------------------------------------------------------
+// Launchers: grid = co-resident blocks (2 per SM at 256 threads), at most the
+// stencil's work; cooperative launch so the barrier cannot wait on a block
+// that is not running.
+// ---------------------------------------------------------------------------
+template <class K> int pcg_resident(K kernel) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find((const void*)kernel);
+  if (it != cache.end()) return it->second;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm <= 0)
+    per_sm = 1;
+  const int n = per_sm * sms;
+  cache.emplace((const void*)kernel, n);
+  return n;
+}
+
+template <class K, class Args> cudaError_t coop_launch(K kernel, int grid, cudaStream_t s, const Args& a) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, a);
+}
+
+int pcg_grid(const Geo& g, int resident) {
+  const int work = g.march ? ((g.nx >> 5) * ((g.nt + kMarchT - 1) / kMarchT) + kBlock / 32 - 1) / (kBlock / 32)
+                           : nblocks(g.V);
+  int grid = resident < work ? resident : work;
+  if (grid > kPcgMaxGrid) grid = kPcgMaxGrid;
+  return grid > 0 ? grid : 1;
+}
+
+cudaError_t pcg64(cudaStream_t s, bool mu0, Pcg64Args a) {
+  const bool unit = a.inv_m2 != 0.0;
+  auto k = mu0 ? (unit ? k_pcg64<true, true> : k_pcg64<true, false>)
+               : (unit ? k_pcg64<false, true> : k_pcg64<false, false>);
+  return coop_launch(k, pcg_grid(a.g, pcg_resident(k)), s, a);
+}
+
+cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a) {
+  auto k = mu0 ? k_pcgmx<true> : k_pcgmx<false>;
+  return coop_launch(k, pcg_grid(a.g, pcg_resident(k)), s, a);
+}
+
+}  // namespace tg

@@ -28,9 +28,10 @@ def _p(a: np.ndarray):
     return a.ctypes.data_as(_dp)
 
 
-def cg_params(rel_tol=0.0, abs_tol2=1e-30, maxiter=100000, precision=N.PREC_FP64, ru_interval=50) -> N.CgParams:
+def cg_params(rel_tol=0.0, abs_tol2=1e-30, maxiter=100000, precision=N.PREC_FP64, ru_interval=50,
+              solver=N.SOLVER_DEFAULT) -> N.CgParams:
     """CG settings; the defaults are hmc.c's (CG_ACCURACY 1e-30 absolute, hmc.c:34-35)."""
-    return N.CgParams(rel_tol, abs_tol2, maxiter, precision, ru_interval, 0)
+    return N.CgParams(rel_tol, abs_tol2, maxiter, precision, ru_interval, solver)
 
 
 def hmc_params(nsteps=10, tau=1.0, npf=1, stochastic_term=True, rng=N.RNG_MT, use_graph=True, seed=0,

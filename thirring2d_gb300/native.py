@@ -12,7 +12,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libthirring_gpu.so")
 
 TG_OK, TG_E_NOCONV, TG_E_DIVERGED, TG_E_NAN, TG_E_CUDA, TG_E_ARG, TG_E_ALLOC = range(7)
-STATUS_NAMES = {0: "OK", 1: "NOCONV", 2: "DIVERGED", 3: "NAN", 4: "CUDA", 5: "ARG", 6: "ALLOC"}
+STATUS_NAMES = {0: "OK", 1: "NOCONV", 2: "DIVERGED", 3: "NAN", 4: "CUDA", 5: "ARG", 6: "ALLOC", 7: "TIMEOUT"}
+SOLVER_DEFAULT, SOLVER_LAUNCHES, SOLVER_PERSISTENT = 0, 1, 2
 BC_PERIODIC, BC_ANTIPERIODIC, BC_OPEN = 1, -1, 0
 PREC_FP64, PREC_MIXED = 0, 1
 RNG_MT, RNG_PHILOX, RNG_EXTERNAL = 0, 1, 2
@@ -25,7 +26,7 @@ class LatticeParams(C.Structure):
 
 class CgParams(C.Structure):
     _fields_ = [("rel_tol", C.c_double), ("abs_tol2", C.c_double), ("maxiter", C.c_int), ("precision", C.c_int),
-                ("ru_interval", C.c_int), ("pad_", C.c_int)]
+                ("ru_interval", C.c_int), ("solver", C.c_int)]
 
 
 class CgResult(C.Structure):
