@@ -213,6 +213,10 @@ int tg_chiral_condensate(tg_lattice* L, const tg_cg_params* cp, int sources, uns
  * 256 threads per SM, CUDA events).  The
  * FP64 roof against which the FP64 operator and CG kernels are reported. */
 int tg_measure_fp64_peak(int device, double* tflops);
+/* Waits of the shared-memory-staged FP32 stencil kernels that gave up (their
+ * bounded wait on a TMA copy ran out) since the library was loaded: 0 in a
+ * healthy run.  No reference counterpart. */
+int tg_stage_faults(int device, unsigned* count);
 
 /* ---- dense matrix and determinant (tiny lattices) ------------------------ */
 /* fermion_matrix (hmc.c:269-310) for the lattice's gauge field, row-major

@@ -635,6 +635,14 @@ extern "C" {
 const char* tg_last_error(void) { return g_err.c_str(); }
 const char* tg_version(void) { return "thirring2d_gb300 0.1 (sm_103a)"; }
 
+int tg_stage_faults(int device, unsigned* count) {
+  if (!count) return fail(TG_E_ARG, "null argument");
+  TG_CK(cudaSetDevice(device));
+  *count = stage_faults();
+  if (*count == 0xffffffffu) return fail(TG_E_CUDA, "cannot read the stage fault counter");
+  return TG_OK;
+}
+
 int tg_measure_fp64_peak(int device, double* tflops) {
   if (!tflops) return fail(TG_E_ARG, "null argument");
   TG_CK(cudaSetDevice(device));

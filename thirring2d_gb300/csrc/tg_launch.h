@@ -157,6 +157,9 @@ struct PcgMxArgs {
 cudaError_t pcg64(cudaStream_t s, bool mu0, Pcg64Args a);
 cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a);
 
+// staged-kernel waits (tg_kernels.cu) that ran out since the library was loaded
+unsigned stage_faults();
+
 // FP64 FMA throughput probe: grid * 256 * 32 * iters FMAs, writes nothing
 void dfma_peak(cudaStream_t s, int grid, int iters, double* sink);
 

@@ -105,6 +105,7 @@ SIGNATURES = {
     "tg_fermion_phase": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "tg_chiral_condensate": (C.c_int, [_vp, C.POINTER(CgParams), C.c_int, C.c_ulonglong, _dp, _dp]),
     "tg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
+    "tg_stage_faults": (C.c_int, [C.c_int, C.POINTER(C.c_uint)]),
     "tg_dense_M": (C.c_int, [_vp, _dp]),
     "tg_log_det": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
     "tg_fm_apply": (C.c_int, [_vp, C.POINTER(C.c_int), _dp, _dp, C.c_int]),
@@ -155,4 +156,11 @@ def fp64_peak_tflops(device: int = 0) -> float:
     """Measured FP64 FMA throughput of the GPU (TFLOP/s, tg_measure_fp64_peak)."""
     v = C.c_double()
     check(load().tg_measure_fp64_peak(device, C.byref(v)))
+    return v.value
+
+
+def stage_faults(device: int = 0) -> int:
+    """Staged-kernel waits that ran out (tg_stage_faults); 0 in a healthy run."""
+    v = C.c_uint()
+    check(load().tg_stage_faults(device, C.byref(v)))
     return v.value
