@@ -290,6 +290,16 @@ def run_ours(args, ws, rank, local):
     dslash_gbs = DSLASH_BYTES_PER_SITE * V / (0.5 * (t_M + t_Md) * 1e-3) / 1e9
     t_M32 = L64.time_apply(20, False, tg.native.PREC_MIXED)
     dslash32_gbs = 32 * V / (t_M32 * 1e-3) / 1e9
+    # the same at 2048^2 (m 0.02, g 0.8, A ~ N(0, 0.5^2)), where the vectors
+    # (32 / 64 MiB) and links no longer fit in L2: the HBM-roofline figures
+    n2 = 2048
+    L2048 = tg.Lattice(n2, n2, 0.02, 0.8, 0.0, W["bc_t"], W["bc_x"], device=local)
+    L2048.set_gauge(np.random.default_rng(2048).normal(0, 0.5, (n2, n2, 2)))
+    t2_M = L2048.time_apply(20, False, tg.native.PREC_FP64)
+    t2_M32 = L2048.time_apply(20, False, tg.native.PREC_MIXED)
+    L2048.close()
+    dslash_2048 = {"fp64_ms": t2_M, "fp64_gbs": 64 * n2 * n2 / (t2_M * 1e-3) / 1e9,
+                   "fp32_ms": t2_M32, "fp32_gbs": 32 * n2 * n2 / (t2_M32 * 1e-3) / 1e9}
 
     # ---- mixed precision on the same field and random stream ----
     Lmx, hpmx = make(tg.native.PREC_MIXED)
@@ -339,7 +349,9 @@ def run_ours(args, ws, rank, local):
                      "frac": fp64_achieved / fp64_peak, "flops_per_site": CG_ITER_FP64_FLOPS_PER_SITE,
                      "note": "the FP64 CG kernels keep the FP64 pipe 85-89% busy (ncu); they are FP64-ALU-bound"},
         "dslash": {"fp64_gbs": dslash_gbs, "fp64_ms_M": t_M, "fp64_ms_Mdag": t_Md, "fp64_frac": dslash_gbs / hbm,
-                   "fp32_gbs": dslash32_gbs, "fp32_ms": t_M32, "bytes_per_site_fp64": 64, "bytes_per_site_fp32": 32},
+                   "fp32_gbs": dslash32_gbs, "fp32_ms": t_M32, "bytes_per_site_fp64": 64, "bytes_per_site_fp32": 32,
+                   "at_2048": dict(dslash_2048, fp64_frac=dslash_2048["fp64_gbs"] / hbm,
+                                   fp32_frac=dslash_2048["fp32_gbs"] / hbm)},
         "mixed": {"value": mixed_value, "unit": "trajectories/s", "speedup_vs_fp64": mixed_value / value,
                   "cg_iterations_per_traj": statistics.mean(r.cg_iterations for r in res_mx),
                   "reliable_updates_per_traj": statistics.mean(r.reliable_updates for r in res_mx),

@@ -218,6 +218,19 @@ int tg_measure_fp64_peak(int device, double* tflops);
  * healthy run.  No reference counterpart. */
 int tg_stage_faults(int device, unsigned* count);
 
+/* ---- fermion-bag propagator matrix ----------------------------------------- */
+/* calc_Dinv with WITH_MASS_MONOMERS (fermion_matrix.c:189-351): for every
+ * source site the column fM^-1 e_src of the masked real operator, each by
+ * cg_propagator (vec_ops.c:311-321, CG on fM^T fM with b = fM^T e_src, the
+ * stopping rules of cp; the reference uses abs_tol2 = 1e-30 and 9999
+ * iterations).  mask: occupation int[V] as for tg_fm_apply, or NULL for the
+ * free propagator.  Dinv: double[V*V/2] laid out as the reference's Dinv
+ * (n = V/2, i = (nx*t + x)/2): Dinv[i2*n + i1] for odd sources i1 and even
+ * sites i2, Dinv[n*n + i2*n + i1] for even sources and odd sites.  A source
+ * whose CG diverges gets 1e50 everywhere, as vec_ops.c:292-296.  res: the
+ * largest iteration count and the worst status.  nx even, V <= 16384. */
+int tg_fm_propagator(tg_lattice* L, const tg_cg_params* cp, const int* mask, double* Dinv, tg_cg_result* res);
+
 /* ---- dense matrix and determinant (tiny lattices) ------------------------ */
 /* fermion_matrix (hmc.c:269-310) for the lattice's gauge field, row-major
  * complex: Md[(i*V + j)*2 + {0,1}] = M_ij with (M psi)_i = sum_j M_ij psi_j.

@@ -147,7 +147,7 @@ def generate_vecops() -> None:
     text = _sub(r"^#define NX 64\s*$", "#define NX REF_NX", text, 1, re.M)
     with open(os.path.join(VSRC, "Thirring.h"), "w") as f:
         f.write("/* GENERATED by oracle/make_ref.py from rantahar/Thirring2D Thirring.h -- do not commit. */\n" + text)
-    for name in ("vec_ops.c", "mersenne_inline.c", "mersenne.h"):
+    for name in ("vec_ops.c", "fermion_matrix.c", "mersenne_inline.c", "mersenne.h"):
         with open(os.path.join(REF_ROOT, name)) as fi, open(os.path.join(VSRC, name), "w") as fo:
             fo.write(fi.read())
     with open(os.path.join(VSRC, "lapacke.h"), "w") as f:
@@ -166,6 +166,30 @@ def build_vec_one(nt: int, nx: int) -> str:
         return out
     cmd = (["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", "-w", "-Wl,-Bsymbolic", f"-I{VSRC}",
             f"-DREF_NT={nt}", f"-DREF_NX={nx}", "-o", out] + srcs + ["-lm"])
+    subprocess.run(cmd, check=True)
+    return out
+
+
+PROP_SIZES = [(8, 8), (6, 4)]
+
+
+def prop_lib_path(nt: int, nx: int) -> str:
+    return os.path.join(OUT, f"libpropref_T{nt}X{nx}.so")
+
+
+def build_prop_one(nt: int, nx: int) -> str:
+    """vec_ops.c + fermion_matrix.c with PROPAGATOR_MATRIX and WITH_MASS_MONOMERS:
+    the reference's calc_Dinv (fermion_matrix.c:189-351).  fermion_matrix.c and
+    Thirring.h both define the neighbour tables, hence -fcommon."""
+    out = prop_lib_path(nt, nx)
+    driver = os.path.join(HERE, "vecops_driver.c")
+    srcs = [driver, os.path.join(VSRC, "vec_ops.c"), os.path.join(VSRC, "fermion_matrix.c"),
+            os.path.join(VSRC, "mersenne_inline.c")]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(s) for s in srcs):
+        return out
+    cmd = (["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", "-w", "-fcommon", "-Wl,-Bsymbolic", f"-I{VSRC}",
+            f"-DREF_NT={nt}", f"-DREF_NX={nx}", "-DPROPAGATOR_MATRIX", "-DWITH_MASS_MONOMERS", "-o", out]
+           + srcs + ["-lm"])
     subprocess.run(cmd, check=True)
     return out
 
@@ -210,6 +234,8 @@ def build(sizes=None, variants=None) -> list[str]:
         libs = list(ex.map(lambda j: build_one(*j), jobs))
         if os.path.exists(os.path.join(VSRC, "vec_ops.c")):
             libs += list(ex.map(lambda j: build_vec_one(*j), VEC_SIZES))
+        if os.path.exists(os.path.join(VSRC, "fermion_matrix.c")):
+            libs += list(ex.map(lambda j: build_prop_one(*j), PROP_SIZES))
     return libs
 
 

@@ -195,6 +195,31 @@ class Oracle:
         self.L.orc_fM(C.byref(self.lat), _ptr(mask, _ip), _ptr(v), _ptr(out), int(transpose))
         return out
 
+    def fm_propagator(self, mask=None, abs_tol2=1e-30, maxiter=9999):
+        """calc_Dinv (fermion_matrix.c:189-351) restated: for every source the column
+        fM^-1 e_src by cg_propagator (vec_ops.c:311-321), the entries on the other
+        parity in the reference's layout double[2, V/2, V/2] (i = (nx*t + x)/2):
+        [0] odd sources / even sites, [1] even sources / odd sites."""
+        nt, nx, V = self.nt, self.nx, self.nt * self.nx
+        mask = np.zeros((nt, nx), np.int32) if mask is None else mask
+        n = V // 2
+        out = np.zeros((2, n, n))
+        for src in range(V):
+            e = np.zeros(V)
+            e[src] = 1.0
+            b = self.fM(mask, e.reshape(nt, nx), True)
+            x, st, _ = self.cg_MdM(mask, b, abs_tol2=abs_tol2, maxiter=maxiter)
+            if st == 2:
+                x = np.full_like(x, 1e50)
+            ts, xs = divmod(src, nx)
+            par = (ts + xs) & 1
+            blk = out[0 if par else 1]
+            for s in range(V):
+                t, xx = divmod(s, nx)
+                if ((t + xx) & 1) != par:
+                    blk[s // 2, src // 2] = x.ravel()[s]
+        return out
+
     def cg_MdM(self, mask, b, rel_tol=0.0, abs_tol2=1e-30, maxiter=100000):
         mask = np.ascontiguousarray(mask, dtype=np.int32)
         b = _f64(b)
@@ -304,16 +329,18 @@ def _ref_dense(self):
 RefHMC.dense_M = _ref_dense
 
 
-def vec_ref_lib_path(nt: int, nx: int) -> str:
-    return os.path.join(REF_DIR, f"libvecopsref_T{nt}X{nx}.so")
+def vec_ref_lib_path(nt: int, nx: int, prop: bool = False) -> str:
+    return os.path.join(REF_DIR, f"libpropref_T{nt}X{nx}.so" if prop else f"libvecopsref_T{nt}X{nx}.so")
 
 
 class RefVecOps:
     """A private instance of the reference's vec_ops.c (fM, fM_transpose,
-    cg_MdM of the fermion-bag programs; ANTISYMMETRIC build)."""
+    cg_MdM of the fermion-bag programs; ANTISYMMETRIC build).  prop=True loads
+    the build with fermion_matrix.c's calc_Dinv (PROPAGATOR_MATRIX,
+    WITH_MASS_MONOMERS)."""
 
-    def __init__(self, nt, nx, m, mu=0.0):
-        src = vec_ref_lib_path(nt, nx)
+    def __init__(self, nt, nx, m, mu=0.0, prop=False):
+        src = vec_ref_lib_path(nt, nx, prop)
         if not os.path.exists(src):
             raise FileNotFoundError(f"{src} not built (python oracle/make_ref.py)")
         self._tmp = tempfile.mkdtemp(prefix="vecref_")
@@ -340,3 +367,17 @@ class RefVecOps:
         x = np.empty_like(b)
         self.L.vref_cg_MdM(_ptr(b), _ptr(x))
         return x
+
+    def calc_Dinv(self):
+        """The reference's propagator matrix for the current field, double[2, V/2, V/2]
+        (calc_Dinv caches it in a file of the working directory: run in an empty one)."""
+        n = self.nt * self.nx // 2
+        out = np.empty((2, n, n))
+        cwd = os.getcwd()
+        work = tempfile.mkdtemp(prefix="dinv_", dir=self._tmp)
+        try:
+            os.chdir(work)
+            self.L.vref_calc_Dinv(_ptr(out))
+        finally:
+            os.chdir(cwd)
+        return out

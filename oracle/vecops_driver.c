@@ -70,3 +70,21 @@ void vref_cg_MdM(const double* b, double* x) {
   cg_MdM(vout, vin);
   from_rows(vout, x);
 }
+
+#ifdef PROPAGATOR_MATRIX
+/* calc_Dinv (fermion_matrix.c:189-351, built with PROPAGATOR_MATRIX and
+ * WITH_MASS_MONOMERS) for the current field; out: double[NT*NX*NT*NX/2] in the
+ * reference's layout.  calc_Dinv reads a cached propagator file from the
+ * working directory if one exists and writes one: call it from an empty
+ * directory. */
+double* Dinv;
+
+void vref_calc_Dinv(double* out) {
+  const size_t n = (size_t)NT * NX * NT * NX / 2;
+  Dinv = malloc(n * sizeof(double));
+  calc_Dinv();
+  for (size_t i = 0; i < n; i++) out[i] = Dinv[i];
+  free(Dinv);
+  Dinv = NULL;
+}
+#endif

@@ -146,10 +146,30 @@ def make_free_det():
                             logabsdet=logabs, sign=sign)
 
 
+PROP_CONFIGS = {  # name: (nt, nx, m, mu, fraction of occupied sites, seed)
+    "prop_8x8": (8, 8, 0.0, 0.2, 0.0, 0),
+    "prop_6x4_mask": (6, 4, 0.3, 0.0, 0.25, 5),
+}
+
+
+def make_prop():
+    """calc_Dinv (fermion_matrix.c:189-351, WITH_MASS_MONOMERS) of the reference:
+    the propagator matrix from one cg_propagator solve per source site."""
+    from oracle.oracle import RefVecOps
+    for name, (nt, nx, m, mu, occ, seed) in PROP_CONFIGS.items():
+        rng = np.random.default_rng(seed)
+        mask = (rng.random((nt, nx)) < occ).astype(np.int32)
+        ref = RefVecOps(nt, nx, m, mu, prop=True)
+        ref.set_field(mask)
+        np.savez_compressed(os.path.join(OUT, f"{name}.npz"), nt=nt, nx=nx, m=m, mu=mu, mask=mask,
+                            Dinv=ref.calc_Dinv())
+
+
 if __name__ == "__main__":
     make_ref.build([(c[0], c[1]) for c in CONFIGS.values()] + [(4, 4), (6, 4)])
     make_vecops()
     make_free_det()
+    make_prop()
     make_mt()
     make_dense()
     for name, cfg in CONFIGS.items():

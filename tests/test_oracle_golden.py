@@ -137,3 +137,13 @@ def test_free_matrix_equals_fermion_bag_matrix(oracle_lib, name):
     assert np.abs(Md - d["M"]).max() < 1e-15
     sign, logabs = np.linalg.slogdet(Md)
     assert abs(logabs - float(d["logabsdet"])) < 1e-12 and abs(sign - float(d["sign"])) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["prop_8x8", "prop_6x4_mask"])
+def test_propagator_oracle(oracle_lib, name):
+    """calc_Dinv (fermion_matrix.c:189-351): the oracle's restatement against the
+    reference's propagator matrix."""
+    d = golden(name)
+    o = oracle_lib.Oracle(int(d["nt"]), int(d["nx"]), float(d["m"]), 0.5, float(d["mu"]), -1, -1)
+    D = o.fm_propagator(d["mask"])
+    assert np.abs(D - d["Dinv"]).max() < 1e-12 * np.abs(d["Dinv"]).max()

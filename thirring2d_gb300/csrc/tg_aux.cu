@@ -325,3 +325,117 @@ void dfma_peak(cudaStream_t s, int grid, int iters, double* sink) {
 }
 
 }  // namespace tg
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// Propagator matrix of the fermion-bag programs: calc_Dinv with
+// WITH_MASS_MONOMERS (fermion_matrix.c:189-351).  For every source site the
+// column fM^-1 e_src comes from cg_propagator (vec_ops.c:311-321): CG on
+// fM^T fM (vec_ops.c:261-307) with b = fM^T e_src.  One block per source, all
+// of a launch's sources at once; every block keeps x, r, p, fM p, fM^T fM p in
+// its own slice of `scratch`.  The entries on the sites of the other parity
+// go to Dinv as the reference stores them (n = V/2, i = (nx*t + x)/2):
+//   Dinv[i2*n + i1]       odd source i1, even site i2
+//   Dinv[n*n + i2*n + i1] even source i1, odd site i2
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double block_allsum(double v) {
+  __shared__ double sh[32];
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();  // the previous call's readers are done with sh
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0;
+  for (int i = 0; i < nw; i++) t += sh[i];  // same order in every thread
+  return t;
+}
+
+__global__ void __launch_bounds__(kBlock) k_prop_cg(PropArgs a) {
+  const Geo& g = a.g;
+  const int V = g.V;
+  const int src = a.src0 + blockIdx.x;
+  double* x = a.scratch + (size_t)blockIdx.x * 5 * V;
+  double* r = x + V;
+  double* p = r + V;
+  double* Mp = p + V;
+  double* MMp = Mp + V;
+  for (int s = threadIdx.x; s < V; s += blockDim.x) {
+    Mp[s] = (s == src) ? 1.0 : 0.0;
+    x[s] = 0.0;
+  }
+  __syncthreads();
+  double v = 0;
+  for (int s = threadIdx.x; s < V; s += blockDim.x) {  // r = p = fM^T e_src
+    const double b = fm_site<1>(g, a.m, a.ep, a.em, a.bc_t, a.bc_x, a.mask, Mp, s);
+    r[s] = b;
+    p[s] = b;
+    v = fma(b, b, v);
+  }
+  double rr_old = block_allsum(v);
+  const double rr_init = rr_old;
+  double stop = a.abs_tol2;
+  if (a.rel_tol > 0 && a.rel_tol * a.rel_tol * rr_init > stop) stop = a.rel_tol * a.rel_tol * rr_init;
+  int status = TG_OK, iters = 0;
+  if (!(rr_old < stop)) {  // vec_ops.c:275-277
+    status = TG_E_NOCONV;
+    while (iters < a.maxiter) {
+      __syncthreads();
+      for (int s = threadIdx.x; s < V; s += blockDim.x)
+        Mp[s] = fm_site<0>(g, a.m, a.ep, a.em, a.bc_t, a.bc_x, a.mask, p, s);
+      __syncthreads();
+      v = 0;
+      for (int s = threadIdx.x; s < V; s += blockDim.x) {
+        const double mm = fm_site<1>(g, a.m, a.ep, a.em, a.bc_t, a.bc_x, a.mask, Mp, s);
+        MMp[s] = mm;
+        v = fma(p[s], mm, v);
+      }
+      const double alpha = rr_old / block_allsum(v);  // rr / <p, fM^T fM p>
+      v = 0;
+      for (int s = threadIdx.x; s < V; s += blockDim.x) {
+        x[s] = fma(alpha, p[s], x[s]);
+        const double rv = fma(-alpha, MMp[s], r[s]);
+        r[s] = rv;
+        v = fma(rv, rv, v);
+      }
+      const double rr = block_allsum(v);
+      iters++;
+      if (isnan(rr)) {
+        status = TG_E_NAN;
+        break;
+      }
+      if (rr < stop) {
+        status = TG_OK;
+        break;
+      }
+      if (rr / rr_init > 1e10) {  // an (almost) exact zero mode: vec_ops.c:292-296 sets the solution to 1e50
+        status = TG_E_DIVERGED;
+        for (int s = threadIdx.x; s < V; s += blockDim.x) x[s] = 1e50;
+        break;
+      }
+      const double beta = rr / rr_old;
+      for (int s = threadIdx.x; s < V; s += blockDim.x) p[s] = fma(beta, p[s], r[s]);
+      rr_old = rr;
+    }
+  }
+  __syncthreads();
+  int ts, xs;
+  site_tx(g, src, ts, xs);
+  const int par = (ts + xs) & 1;
+  const int n = V / 2;
+  double* out = a.Dinv + (par ? 0 : (size_t)n * n);
+  const int i1 = src / 2;
+  for (int s = threadIdx.x; s < V; s += blockDim.x) {
+    int t, xx;
+    site_tx(g, s, t, xx);
+    if (((t + xx) & 1) != par) out[(size_t)(s / 2) * n + i1] = x[s];
+  }
+  if (threadIdx.x == 0) {
+    atomicMax(a.max_iter, iters);
+    atomicMax(a.worst, status);
+  }
+}
+
+void prop_cg(cudaStream_t s, int nsrc, const PropArgs& a) { k_prop_cg<<<nsrc, kBlock, 0, s>>>(a); }
+
+}  // namespace tg

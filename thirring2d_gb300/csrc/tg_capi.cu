@@ -1181,6 +1181,70 @@ int tg_cg_mdm_masked(tg_lattice* L, const tg_cg_params* cp, const int* mask, con
   return solver_status(L->h_st->status);
 }
 
+int tg_fm_propagator(tg_lattice* L, const tg_cg_params* cp, const int* mask, double* Dinv, tg_cg_result* res) {
+  if (!L || !Dinv) return fail(TG_E_ARG, "null argument");
+  TG_TRY(check_cg_params(cp));
+  if (L->P.nx % 2 != 0) return fail(TG_E_ARG, "the propagator matrix needs an even nx");
+  if (L->V > 16384) return fail(TG_E_ARG, "the propagator matrix is for lattices of at most 16384 sites");
+  TG_TRY(ensure_real(L));
+  const int V = L->V;
+  if (mask) {
+    TG_TRY(upload_mask(L, mask));
+  } else {
+    TG_CK(cudaMemsetAsync(L->mask, 0, sizeof(int) * V, L->stream));
+  }
+  const size_t nD = (size_t)V * V / 2;
+  // sources per launch: their CG vectors (5 V doubles each) within 1 GiB
+  const size_t per_src = 5 * (size_t)V;
+  int nb = (int)std::min<size_t>((size_t)V, std::max<size_t>(1, ((size_t)1 << 27) / per_src));
+  double *dD = nullptr, *scratch = nullptr;
+  int* stats = nullptr;
+  TG_TRY(dmalloc(&dD, nD));
+  int rc = dmalloc(&scratch, per_src * nb);
+  if (rc == TG_OK) rc = dmalloc(&stats, 2);
+  if (rc == TG_OK && cudaMemsetAsync(stats, 0, 2 * sizeof(int), L->stream) != cudaSuccess)
+    rc = fail(TG_E_CUDA, "memset failed");
+  if (rc == TG_OK) {
+    PropArgs a{};
+    a.g = L->g;
+    a.m = L->P.m;
+    a.ep = exp(L->P.mu);
+    a.em = exp(-L->P.mu);
+    a.bc_t = L->P.bc_t;
+    a.bc_x = L->P.bc_x;
+    a.mask = L->mask;
+    a.scratch = scratch;
+    a.Dinv = dD;
+    a.abs_tol2 = cp->abs_tol2;
+    a.rel_tol = cp->rel_tol;
+    a.maxiter = cp->maxiter;
+    a.max_iter = stats;
+    a.worst = stats + 1;
+    for (int src0 = 0; src0 < V && rc == TG_OK; src0 += nb) {
+      a.src0 = src0;
+      prop_cg(L->stream, std::min(nb, V - src0), a);
+      if (cudaGetLastError() != cudaSuccess) rc = fail(TG_E_CUDA, "propagator kernel launch failed");
+    }
+  }
+  int h[2] = {0, 0};
+  if (rc == TG_OK && (cudaMemcpyAsync(Dinv, dD, nD * sizeof(double), cudaMemcpyDeviceToHost, L->stream) != cudaSuccess ||
+                      cudaMemcpyAsync(h, stats, sizeof h, cudaMemcpyDeviceToHost, L->stream) != cudaSuccess ||
+                      cudaStreamSynchronize(L->stream) != cudaSuccess))
+    rc = fail(TG_E_CUDA, "propagator matrix failed");
+  cudaFree(dD);
+  if (scratch) cudaFree(scratch);
+  if (stats) cudaFree(stats);
+  if (rc != TG_OK) return rc;
+  if (res) {
+    res->iterations = h[0];
+    res->status = h[1];
+    res->reliable_updates = 0;
+    res->rr = 0;
+    res->rr0 = 0;
+  }
+  return solver_status(h[1]);
+}
+
 int tg_dense_M(tg_lattice* L, double* Md) {
   if (!L || !Md) return fail(TG_E_ARG, "null argument");
   if (L->V > 4096) return fail(TG_E_ARG, "dense M only for lattices of at most 4096 sites");

@@ -160,6 +160,22 @@ cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a);
 // staged-kernel waits (tg_kernels.cu) that ran out since the library was loaded
 unsigned stage_faults();
 
+// Propagator matrix (calc_Dinv): one CG per source site, one block per source
+struct PropArgs {
+  Geo g;
+  double m, ep, em;
+  int bc_t, bc_x;
+  const int* mask;
+  int src0;         // first source site of this launch
+  double* scratch;  // [sources of the launch][5][V]
+  double* Dinv;     // [2][V/2][V/2]
+  double abs_tol2, rel_tol;
+  int maxiter;
+  int* max_iter;    // atomicMax of the iterations of every source
+  int* worst;       // atomicMax of the statuses
+};
+void prop_cg(cudaStream_t s, int nsrc, const PropArgs& a);
+
 // FP64 FMA throughput probe: grid * 256 * 32 * iters FMAs, writes nothing
 void dfma_peak(cudaStream_t s, int grid, int iters, double* sink);
 

@@ -187,6 +187,20 @@ class Lattice:
                                               seed, C.byref(v), C.byref(e)))
         return v.value, e.value
 
+    def fm_propagator(self, mask=None, cp: N.CgParams | None = None):
+        """calc_Dinv (fermion_matrix.c:189-351): Dinv as double[2, V/2, V/2] in the
+        reference's layout, and the CgResult (largest iteration count, worst status)."""
+        n = self.V // 2
+        out = np.empty((2, n, n))
+        res = N.CgResult()
+        mp = None
+        if mask is not None:
+            mask = np.ascontiguousarray(mask, dtype=np.int32).reshape(self.nt, self.nx)
+            mp = mask.ctypes.data_as(C.POINTER(C.c_int))
+        N.check(self.lib.tg_fm_propagator(self.h, C.byref(cp or cg_params(maxiter=9999)), mp, _p(out),
+                                          C.byref(res)), True)
+        return out, res
+
     # -- dense matrix and determinant (hmc.c:269-336) -------------------------
     def fermion_matrix(self) -> np.ndarray:
         out = np.empty((self.V, self.V), np.complex128)

@@ -106,6 +106,7 @@ SIGNATURES = {
     "tg_chiral_condensate": (C.c_int, [_vp, C.POINTER(CgParams), C.c_int, C.c_ulonglong, _dp, _dp]),
     "tg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
     "tg_stage_faults": (C.c_int, [C.c_int, C.POINTER(C.c_uint)]),
+    "tg_fm_propagator": (C.c_int, [_vp, C.POINTER(CgParams), C.POINTER(C.c_int), _dp, C.POINTER(CgResult)]),
     "tg_dense_M": (C.c_int, [_vp, _dp]),
     "tg_log_det": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
     "tg_fm_apply": (C.c_int, [_vp, C.POINTER(C.c_int), _dp, _dp, C.c_int]),
