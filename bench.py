@@ -135,13 +135,20 @@ def barrier(ws):
 
 
 def allmax(ws, v: float) -> float:
+    """The maximum of v over the ranks (the slowest replica's time)."""
     if ws == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_seed(rank: int) -> int:
+    """Each rank runs an independent chain: its own gauge field and Philox key."""
+    return W["seed"] + rank
 
 
 # ---------------------------------------------------------------------------
@@ -228,7 +235,7 @@ def run_ours(args, ws, rank, local):
     dev = torch.device("cuda", local)
     nt, nx = W["nt"], W["nx"]
     V = nt * nx
-    rng = np.random.default_rng(W["seed"] + rank)
+    rng = np.random.default_rng(replica_seed(rank))
     A0 = rng.normal(0, W["sigma"], (nt, nx, 2))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -237,7 +244,7 @@ def run_ours(args, ws, rank, local):
         L.set_gauge(A0)
         cg = tg.cg_params(rel_tol=W["rel_tol"], abs_tol2=0.0, precision=precision, ru_interval=50)
         hp = tg.hmc_params(nsteps=W["nsteps"], tau=W["tau"], npf=W["npf"], stochastic_term=True,
-                           rng=tg.native.RNG_PHILOX, seed=W["seed"] + rank, use_graph=True, cg=cg)
+                           rng=tg.native.RNG_PHILOX, seed=replica_seed(rank), use_graph=True, cg=cg)
         return L, hp
 
     def timed_loop(L, hp, steps, warmup):

@@ -189,6 +189,23 @@ def test_cg_edge_cases(tg):
         L.fmdm_invert_cg(bad, tg.cg_params(maxiter=0))
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cg_singular_operator_is_reported(tg, precision):
+    """m = 0 with t and x periodic and A = 0: the free staggered operator has
+    exact zero modes, so M^dag M x = b has no solution for a generic b.  The
+    solve must end with a failure status (hmc.c:383-386 stops with "Cannot
+    invert fermion matrix"; NaN and the iteration cap are reported too), and
+    the lattice stays usable."""
+    rng = np.random.default_rng(2)
+    L = tg.Lattice(8, 8, 0.0, 0.5, 0.0, 1, 1)
+    b = cplx(rng, (8, 8))
+    x, res = L.fmdm_invert_cg(b, tg.cg_params(rel_tol=1e-12, abs_tol2=0, maxiter=5000, precision=precision))
+    assert res.status in (tg.native.TG_E_DIVERGED, tg.native.TG_E_NAN, tg.native.TG_E_NOCONV)
+    L.set_couplings(0.3, 0.5, 0.0)
+    x, res = L.fmdm_invert_cg(b, tg.cg_params(rel_tol=1e-10, abs_tol2=0, precision=precision))
+    assert res.status == 0
+
+
 def test_cg_mixed_vs_fp64(tg):
     d = golden("c1_16x16_px")
     L = make(tg, d)

@@ -11,7 +11,7 @@ import os
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libthirring_gpu.so")
 
-TG_OK, TG_E_NOCONV, TG_E_DIVERGED, TG_E_NAN, TG_E_CUDA, TG_E_ARG, TG_E_ALLOC = range(7)
+TG_OK, TG_E_NOCONV, TG_E_DIVERGED, TG_E_NAN, TG_E_CUDA, TG_E_ARG, TG_E_ALLOC, TG_E_TIMEOUT = range(8)
 STATUS_NAMES = {0: "OK", 1: "NOCONV", 2: "DIVERGED", 3: "NAN", 4: "CUDA", 5: "ARG", 6: "ALLOC", 7: "TIMEOUT"}
 SOLVER_DEFAULT, SOLVER_LAUNCHES, SOLVER_PERSISTENT = 0, 1, 2
 BC_PERIODIC, BC_ANTIPERIODIC, BC_OPEN = 1, -1, 0
