@@ -1,7 +1,8 @@
 """The FP32 stencil kernels with their rows staged through shared memory by
 TMA bulk copies (TG_STAGED=1, on lattices with nx a multiple of 32) against
 the same kernels loading from global memory (the default): the arithmetic is
-the same, so results are bitwise equal; and no staged wait ever ran out."""
+the same, so operator applies are bitwise equal and solves agree to the rounding
+of their grid sums; and no staged wait ever ran out."""
 import numpy as np
 import pytest
 
@@ -48,7 +49,7 @@ def test_staged_apply_bitwise(tg, monkeypatch, nt, nx, mu):
 
 
 @pytest.mark.parametrize("nt,nx", [(64, 64), (1024, 1024)])
-def test_staged_mixed_cg_bitwise(tg, monkeypatch, nt, nx):
+def test_staged_mixed_cg_agrees(tg, monkeypatch, nt, nx):
     rng = np.random.default_rng(7 * nt)
     A = rng.normal(0, 0.3, (nt, nx, 2))
     b = cplx(rng, (nt, nx))
@@ -61,7 +62,10 @@ def test_staged_mixed_cg_bitwise(tg, monkeypatch, nt, nx):
         L.close()
     (x1, r1), (x0, r0) = res["1"], res["0"]
     assert r1.status == r0.status == 0
-    assert r1.iterations == r0.iterations and r1.reliable_updates == r0.reliable_updates
-    assert np.array_equal(x1, x0)
+    # same arithmetic per site; the two kernels may run on different grids
+    # (the staged one is limited by shared memory), so the per-block partial
+    # sums of the dot products, and with them the last bits, can differ
+    assert abs(r1.iterations - r0.iterations) <= 2
+    assert np.linalg.norm(x1 - x0) / np.linalg.norm(x0) < 1e-7
     assert tg.native.stage_faults() == 0
 

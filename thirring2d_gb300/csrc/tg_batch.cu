@@ -21,7 +21,7 @@
 #include <vector>
 
 #include "tg_batch.h"
-#include "tg_device.cuh"
+#include "tg_stencil.cuh"
 
 namespace tg {
 
@@ -53,8 +53,8 @@ struct ChainCtx {
   int bc_t, bc_x;
   unsigned long long seed;
   // this chain's slices of the packed fields
-  double2 *A, *An, *mom, *phi, *noise, *x, *Mx, *tmp, *Wt, *Wx, *r64, *p64, *Mp64;
-  float2 *Wt32, *Wx32, *xs, *rs, *ps, *Mps;
+  double2 *A, *An, *mom, *phi, *noise, *x, *Mx, *tmp, *Wt, *Wx, *r64, *p64, *p64b, *Mp64;
+  float2 *Wt32, *Wx32, *xs, *rs, *ps, *ps2, *Mps;
 };
 
 struct CgOut {
@@ -88,24 +88,29 @@ __device__ CgOut block_cg64(const ChainCtx& c, const BatchCg& P, const double2* 
     return out;
   }
   double rr = rr0, beta = 0;
+  int half = 0;
   while (true) {
+    // p' = r + beta p formed where the stencil reads it (p of the previous
+    // iteration in one buffer, p' stored at its own site in the other)
+    const double2* p_old = half ? c.p64b : c.p64;
+    double2* p_new = half ? c.p64 : c.p64b;
     double v = 0;
-    TG_BSITES(s, V) {  // p = r + beta p (own site)
-      double2 rv = c.r64[s], pv = c.p64[s];
-      c.p64[s] = make_double2(fma(beta, pv.x, rv.x), fma(beta, pv.y, rv.y));
-    }
-    __syncthreads();
-    TG_BSITES(s, V) {
-      double2 o = dslash_at<double, 0, MU0>(c.g, km, c.p64, c.Wt, c.Wx, s);
+    auto ld = [&](int i) {
+      const double2 rv = c.r64[i], pv = p_old[i];
+      return make_double2(fma(beta, pv.x, rv.x), fma(beta, pv.y, rv.y));
+    };
+    auto epi = [&](int s, double2 o, double2 pc) {
+      p_new[s] = pc;
       c.Mp64[s] = o;
       v = fma(o.x, o.x, v);
       v = fma(o.y, o.y, v);
-    }
+    };
+    stencil_block<double, 0, MU0>(c.g, km, ld, c.Wt, c.Wx, epi);
     const double alpha = rr / bsum(v);
     v = 0;
-    TG_BSITES(s, V) {
-      double2 ap = dslash_at<double, 1, MU0>(c.g, kd, c.Mp64, c.Wt, c.Wx, s);
-      double2 xv = x[s], pv = c.p64[s], rv = c.r64[s];
+    auto ld2 = [&](int i) { return c.Mp64[i]; };
+    auto epi2 = [&](int s, double2 ap, double2) {
+      double2 xv = x[s], pv = p_new[s], rv = c.r64[s];
       xv.x += alpha * pv.x;
       xv.y += alpha * pv.y;
       rv.x -= alpha * ap.x;
@@ -114,8 +119,10 @@ __device__ CgOut block_cg64(const ChainCtx& c, const BatchCg& P, const double2* 
       c.r64[s] = rv;
       v = fma(rv.x, rv.x, v);
       v = fma(rv.y, rv.y, v);
-    }
+    };
+    stencil_block<double, 1, MU0>(c.g, kd, ld2, c.Wt, c.Wx, epi2);
     const double rn = bsum(v);
+    half ^= 1;
     out.iter++;
     beta = rn / rr;
     rr = rn;
@@ -152,27 +159,29 @@ __device__ CgOut block_cg_mixed(const ChainCtx& c, const BatchCg& P, const doubl
     return out;
   }
   double rr = rr0, rr_true = rr0, beta = 0;
-  int since = 0;
+  int since = 0, half = 0;
   while (true) {
     const float fb = (float)beta;
-    TG_BSITES(s, V) {
-      float2 rv = c.rs[s], pv = c.ps[s];
-      c.ps[s] = make_float2(fmaf(fb, pv.x, rv.x), fmaf(fb, pv.y, rv.y));
-    }
-    __syncthreads();
+    const float2* p_old = half ? c.ps2 : c.ps;
+    float2* p_new = half ? c.ps : c.ps2;
     float v = 0;
-    TG_BSITES(s, V) {
-      float2 o = dslash_at<float, 0, MU0>(c.g, km32, c.ps, c.Wt32, c.Wx32, s);
+    auto ld = [&](int i) {
+      const float2 rv = c.rs[i], pv = p_old[i];
+      return make_float2(fmaf(fb, pv.x, rv.x), fmaf(fb, pv.y, rv.y));
+    };
+    auto epi = [&](int s, float2 o, float2 pc) {
+      p_new[s] = pc;
       c.Mps[s] = o;
       v = fmaf(o.x, o.x, v);
       v = fmaf(o.y, o.y, v);
-    }
+    };
+    stencil_block<float, 0, MU0>(c.g, km32, ld, c.Wt32, c.Wx32, epi);
     const double alpha = rr / bsum((double)v);
     const float fa = (float)alpha;
     v = 0;
-    TG_BSITES(s, V) {
-      float2 ap = dslash_at<float, 1, MU0>(c.g, kd32, c.Mps, c.Wt32, c.Wx32, s);
-      float2 xv = c.xs[s], pv = c.ps[s], rv = c.rs[s];
+    auto ld2 = [&](int i) { return c.Mps[i]; };
+    auto epi2 = [&](int s, float2 ap, float2) {
+      float2 xv = c.xs[s], pv = p_new[s], rv = c.rs[s];
       xv.x = fmaf(fa, pv.x, xv.x);
       xv.y = fmaf(fa, pv.y, xv.y);
       rv.x = fmaf(-fa, ap.x, rv.x);
@@ -181,8 +190,10 @@ __device__ CgOut block_cg_mixed(const ChainCtx& c, const BatchCg& P, const doubl
       c.rs[s] = rv;
       v = fmaf(rv.x, rv.x, v);
       v = fmaf(rv.y, rv.y, v);
-    }
+    };
+    stencil_block<float, 1, MU0>(c.g, kd32, ld2, c.Wt32, c.Wx32, epi2);
     const double rn = bsum((double)v);
+    half ^= 1;
     out.iter++;
     since++;
     beta = rn / rr;
@@ -379,16 +390,16 @@ __device__ __forceinline__ void fill_ctx(ChainCtx& c, const BatchChain& b, const
     const long long o = b.off;
     c.A = F.A + o; c.An = F.An + o; c.mom = F.mom + o; c.phi = F.phi + o; c.noise = F.noise + o;
     c.x = F.x + o; c.Mx = F.Mx + o; c.tmp = F.tmp + o; c.Wt = F.Wt + o; c.Wx = F.Wx + o;
-    c.r64 = F.r64 + o; c.p64 = F.p64 + o; c.Mp64 = F.Mp64 + o;
+    c.r64 = F.r64 + o; c.p64 = F.p64 + o; c.p64b = F.p64b + o; c.Mp64 = F.Mp64 + o;
     c.Wt32 = F.Wt32 + o; c.Wx32 = F.Wx32 + o; c.xs = F.xs + o; c.rs = F.rs + o; c.ps = F.ps + o;
-    c.Mps = F.Mps + o;
+    c.ps2 = F.ps2 + o; c.Mps = F.Mps + o;
 }
 
 // The kernel instances the autotuner chooses from: (threads per block,
 // minimum resident blocks per SM).  More blocks per SM cap the registers (64 at
-// 2048 resident threads, with small spills in the reliable-update path);
-// fewer leave them uncapped (about 120).
-const BatchCfg kBatchCfgs[kBatchNumCfgs] = {{128, 8}, {256, 4}, {256, 2}, {384, 2}, {512, 2}, {512, 1}};
+// 2048 resident threads, with spills in the column march); fewer leave room
+// for the march's registers (up to 255 at 256 threads and one block).
+const BatchCfg kBatchCfgs[kBatchNumCfgs] = {{128, 8}, {256, 4}, {256, 2}, {256, 1}, {384, 1}, {512, 1}};
 
 template <int BS, int MINB> const void* batch_kernel() { return (const void*)k_batch_trajectory<BS, MINB>; }
 
@@ -397,8 +408,8 @@ static const void* batch_kernel_of(int cfg) {
     case 0: return batch_kernel<128, 8>();
     case 1: return batch_kernel<256, 4>();
     case 2: return batch_kernel<256, 2>();
-    case 3: return batch_kernel<384, 2>();
-    case 4: return batch_kernel<512, 2>();
+    case 3: return batch_kernel<256, 1>();
+    case 4: return batch_kernel<384, 1>();
     default: return batch_kernel<512, 1>();
   }
 }
@@ -409,8 +420,8 @@ void batch_trajectory(cudaStream_t s, int cfg, int grid, const BatchChain* chain
     case 0: k_batch_trajectory<128, 8><<<grid, 128, 0, s>>>(chains, order, n, F, P, results, queue); break;
     case 1: k_batch_trajectory<256, 4><<<grid, 256, 0, s>>>(chains, order, n, F, P, results, queue); break;
     case 2: k_batch_trajectory<256, 2><<<grid, 256, 0, s>>>(chains, order, n, F, P, results, queue); break;
-    case 3: k_batch_trajectory<384, 2><<<grid, 384, 0, s>>>(chains, order, n, F, P, results, queue); break;
-    case 4: k_batch_trajectory<512, 2><<<grid, 512, 0, s>>>(chains, order, n, F, P, results, queue); break;
+    case 3: k_batch_trajectory<256, 1><<<grid, 256, 0, s>>>(chains, order, n, F, P, results, queue); break;
+    case 4: k_batch_trajectory<384, 1><<<grid, 384, 0, s>>>(chains, order, n, F, P, results, queue); break;
     default: k_batch_trajectory<512, 1><<<grid, 512, 0, s>>>(chains, order, n, F, P, results, queue); break;
   }
 }

@@ -18,8 +18,8 @@ struct BatchChain {
 
 // Packed per-site fields of all chains.
 struct BatchFields {
-  double2 *A, *An, *mom, *phi, *noise, *x, *Mx, *tmp, *Wt, *Wx, *r64, *p64, *Mp64;
-  float2 *Wt32, *Wx32, *xs, *rs, *ps, *Mps;
+  double2 *A, *An, *mom, *phi, *noise, *x, *Mx, *tmp, *Wt, *Wx, *r64, *p64, *p64b, *Mp64;
+  float2 *Wt32, *Wx32, *xs, *rs, *ps, *ps2, *Mps;  // p64/p64b, ps/ps2: CG directions of alternate iterations
 };
 
 struct BatchCg {

@@ -1483,10 +1483,10 @@ int tg_batch_create(const tg_chain_params* chains, int nchains, int device, tg_b
   if (B->sms <= 0) B->sms = 1;
   int rc;
   double2** d2[] = {&B->F.A, &B->F.An, &B->F.mom, &B->F.phi, &B->F.noise, &B->F.x, &B->F.Mx, &B->F.tmp,
-                    &B->F.Wt, &B->F.Wx, &B->F.r64, &B->F.p64, &B->F.Mp64};
+                    &B->F.Wt, &B->F.Wx, &B->F.r64, &B->F.p64, &B->F.p64b, &B->F.Mp64};
   for (auto pp : d2)
     if ((rc = dmalloc(pp, (size_t)total)) != TG_OK) return bail(rc);
-  float2** f2[] = {&B->F.Wt32, &B->F.Wx32, &B->F.xs, &B->F.rs, &B->F.ps, &B->F.Mps};
+  float2** f2[] = {&B->F.Wt32, &B->F.Wx32, &B->F.xs, &B->F.rs, &B->F.ps, &B->F.ps2, &B->F.Mps};
   for (auto pp : f2)
     if ((rc = dmalloc(pp, (size_t)total)) != TG_OK) return bail(rc);
   if ((rc = dmalloc(&B->d_chains, nchains)) != TG_OK || (rc = dmalloc(&B->d_order, nchains)) != TG_OK ||
@@ -1516,7 +1516,8 @@ int tg_batch_destroy(tg_batch* B) {
     if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
   }
   void* dev[] = {B->F.A, B->F.An, B->F.mom, B->F.phi, B->F.noise, B->F.x, B->F.Mx, B->F.tmp, B->F.Wt, B->F.Wx,
-                 B->F.r64, B->F.p64, B->F.Mp64, B->F.Wt32, B->F.Wx32, B->F.xs, B->F.rs, B->F.ps, B->F.Mps,
+                 B->F.r64, B->F.p64, B->F.p64b, B->F.Mp64, B->F.Wt32, B->F.Wx32, B->F.xs, B->F.rs, B->F.ps,
+                 B->F.ps2, B->F.Mps,
                  B->d_chains, B->d_order, B->d_res, B->d_queue};
   for (void* d : dev)
     if (d) cudaFree(d);

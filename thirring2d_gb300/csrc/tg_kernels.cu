@@ -19,6 +19,11 @@
 
 namespace tg {
 
+// Minimum resident blocks per SM of the stencil kernels: FP32 ones are
+// latency-bound and get more warps; FP64 ones are pipe-bound.
+#define TG_FP32_BLOCKS_PER_SM 3
+template <typename R> constexpr int kFp32BlocksPerSM = sizeof(R) == 4 ? TG_FP32_BLOCKS_PER_SM : kStencilBlocksPerSM;
+
 __global__ void __launch_bounds__(kBlock) k_link_phase(Geo g, int bc_t, int bc_x, const double2* __restrict__ A,
                                                        LinkOut o) {
   TG_SITES(s, g.V) write_links(g, bc_t, bc_x, s, A[s], o);
@@ -112,7 +117,7 @@ bool staged_enabled(const Geo& g) {
 }
 
 template <typename R, int DAG, bool MU0, bool STAGED = false>
-__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_dslash(Geo g, OpK<R> k, const C2<R>* __restrict__ in,
+__global__ void __launch_bounds__(kBlock, kFp32BlocksPerSM<R>) k_dslash(Geo g, OpK<R> k, const C2<R>* __restrict__ in,
                                                    C2<R>* __restrict__ out, const C2<R>* __restrict__ Wt,
                                                    const C2<R>* __restrict__ Wx) {
   auto epi = [&](int s, C2<R> o, C2<R>) { out[s] = o; };
@@ -233,7 +238,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(Geo g, const double2* __rest
 }
 
 template <typename R, bool MU0, bool UNIT = false, bool STAGED = false>
-__global__ void __launch_bounds__(kBlock, 2) k_cg1(Geo g, OpK<R> k, const C2<R>* __restrict__ r,
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? kFp32BlocksPerSM<R> : 2) k_cg1(Geo g, OpK<R> k, const C2<R>* __restrict__ r,
                                                 const C2<R>* __restrict__ p_old, C2<R>* __restrict__ p_new,
                                                 C2<R>* __restrict__ Mp, const C2<R>* __restrict__ Wt,
                                                 const C2<R>* __restrict__ Wx, CgState* st, Red red) {
@@ -331,7 +336,7 @@ void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<do
 // the last one, when the FP32 residual reaches the target, and at the cap.
 // ---------------------------------------------------------------------------
 template <bool MU0, bool STAGED = false>
-__global__ void __launch_bounds__(kBlock, kStencilBlocksPerSM) k_cgmx2(Geo g, OpK<float> k, const float2* __restrict__ Mp,
+__global__ void __launch_bounds__(kBlock, kFp32BlocksPerSM<float>) k_cgmx2(Geo g, OpK<float> k, const float2* __restrict__ Mp,
                                                   const float2* __restrict__ p, float2* __restrict__ xs,
                                                   float2* __restrict__ r, const float2* __restrict__ Wt,
                                                   const float2* __restrict__ Wx, CgState* st, Red red, Cond c) {

@@ -136,6 +136,37 @@ __device__ __forceinline__ void stencil_all(const Geo& g, const OpK<R>& k, const
   stencil_ld<R, DAG, MU0, UNIT>(g, k, ld, Wt, Wx, epi);
 }
 
+// The operator over one small lattice inside one thread block (the batched-chain
+// kernel): the block's warps split the lattice's (strip, t) rows into one
+// contiguous range each, as for_warp_rows splits them over a grid; lattices
+// whose nx is not a multiple of 32 go one site per thread.
+template <typename R, int DAG, bool MU0, class Ld, class Epi>
+__device__ __forceinline__ void stencil_block(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
+                                              const C2<R>* __restrict__ Wx, Epi& epi) {
+  if ((g.nx & 31) == 0) {
+    const int nw = blockDim.x >> 5, w = threadIdx.x >> 5;
+    const int rows = (g.nx >> 5) * g.nt;
+    int r = (int)((long long)rows * w / nw);
+    const int r1 = (int)((long long)rows * (w + 1) / nw);
+    while (r < r1) {
+      const int xw = r / g.nt;
+      const int ta = r - xw * g.nt;
+      const int tb = (r1 - r < g.nt - ta) ? ta + (r1 - r) : g.nt;
+      march_segment<R, DAG, MU0>(g, k, ld, Wt, Wx, xw, ta, tb, epi);
+      r += tb - ta;
+    }
+  } else {
+    for (int s = threadIdx.x; s < g.V; s += blockDim.x) {
+      int t, x;
+      site_tx(g, s, t, x);
+      const Nbr n = neighbours(g, s, t, x);
+      const C2<R> pc = ld(s);
+      epi(s, dslash_vals<R, DAG, MU0>(k, pc, ld(n.tp), ld(n.tm), ld(n.xp), ld(n.xm), Wt[s], Wt[n.tm], Wx[s], Wx[n.xm]),
+          pc);
+    }
+  }
+}
+
 // Blocks of work of a stencil kernel (march: at least kMarchT rows per warp).
 inline int stencil_work(const Geo& g) {
   return g.march ? ((g.nx >> 5) * ((g.nt + kMarchT - 1) / kMarchT) + kBlock / 32 - 1) / (kBlock / 32) : nblocks(g.V);
