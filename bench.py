@@ -351,7 +351,10 @@ def run_ours(args, ws, rank, local):
                      "peak_source": peak_kind, "bytes_per_site": CG_ITER_BYTES_PER_SITE,
                      "ms_per_iteration": t_iter_ms,
                      "traffic": CG_ITER_DRAM_BYTES,
-                     "traffic_source": "profiles/cg_iteration_1024_fp64.md (ncu, one capture)"},
+                     "traffic_source": "profiles/cg_iteration_1024_fp64.md (ncu, one capture)",
+                     "note": "the FP64 CG kernels are bound by the FP64 pipe, not HBM: fp64_alu.frac is the "
+                             "fraction of the measured FP64 FMA rate; dslash.at_2048.fp32_frac is the "
+                             "HBM-bound FP32 stencil's"},
         "fp64_alu": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak, "peak_source": fp64_peak_kind,
                      "frac": fp64_achieved / fp64_peak, "flops_per_site": CG_ITER_FP64_FLOPS_PER_SITE,
                      "note": "the FP64 CG kernels keep the FP64 pipe 85-89% busy (ncu); they are FP64-ALU-bound"},
