@@ -334,10 +334,13 @@ void launch_k(void (*kernel)(Exp...), int grid, cudaStream_t s, bool pdl, Act&&.
   cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
 }
 
-// TG_PDL=0 turns the programmatic dependencies of the FP64 CG kernels off
+// TG_PDL=1 turns on programmatic dependencies between the FP64 CG kernels.
+// Off by default: at 1024^2 the iteration measured 94.3 us with them against
+// 93.6 us without (the early-launched blocks of the next kernel take SM slots
+// while this one's tail runs).
 bool pdl_enabled() {
   const char* e = getenv("TG_PDL");
-  return !(e && e[0] == '0');
+  return e && e[0] == '1';
 }
 
 void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
