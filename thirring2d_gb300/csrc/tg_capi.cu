@@ -364,7 +364,7 @@ int enqueue_cg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const doub
     TG_CK(cudaStreamBeginCaptureToGraph(L->cap2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     for (int half = 0; half < 2; half++) {
       if (!mixed) {
-        cg64_iter(L->cap2, g, km, kd, lk, x, L->w64, half, L->st, L->log, L->red, c0, half == 1);
+        cg64_iter(L->cap2, g, km, kd, lk, x, L->w64, half, L->st, L->log, L->red, c0);
       } else {
         cudaGraphConditionalHandle hru;
         TG_CK(cudaGraphConditionalHandleCreate(&hru, body, 0, 0));
@@ -400,7 +400,7 @@ int enqueue_cg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const doub
     for (int j = 0; j < chunk; j++) {  // chunk is even: p ends in buffer 0 again
       const int half = j & 1;
       if (!mixed) {
-        cg64_iter(s, g, km, kd, lk, x, L->w64, half, L->st, L->log, L->red, none, j > 0);
+        cg64_iter(s, g, km, kd, lk, x, L->w64, half, L->st, L->log, L->red, none);
       } else {
         cgmx_iter(s, g, km32, kd32, lk, L->wmx, half, L->st, L->red, none);
         cgmx_reliable(s, g, km, kd, lk, b, x, L->wmx, L->st, L->log, L->red, none);

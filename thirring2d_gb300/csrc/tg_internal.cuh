@@ -157,13 +157,6 @@ __device__ __forceinline__ bool grid_sum(T v, double* partials, unsigned* counte
   return true;
 }
 
-// Programmatic dependent launch (sm_90 and later).  pdl_wait: wait until the
-// grid this one was launched after has completed and its writes are visible (a
-// no-op when there is no programmatic dependency).  pdl_release: let the grid
-// launched after this one start while this one finishes.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
 inline int nblocks(int n, int bs = kBlock) { return (n + bs - 1) / bs; }
 inline int grid_of(const Geo& g) { return g.grid; }
 inline int stream_grid(int n) { return nblocks(n); }  // streaming kernels without reductions

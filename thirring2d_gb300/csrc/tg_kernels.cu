@@ -13,7 +13,6 @@
 #include <string.h>
 
 #include <mutex>
-#include <utility>
 #include <unordered_map>
 
 #include "tg_stencil.cuh"
@@ -243,7 +242,6 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? kFp32BlocksPerSM<R> :
                                                 const C2<R>* __restrict__ p_old, C2<R>* __restrict__ p_new,
                                                 C2<R>* __restrict__ Mp, const C2<R>* __restrict__ Wt,
                                                 const C2<R>* __restrict__ Wx, CgState* st, Red red) {
-  pdl_wait();
   if (st->done) return;
   const R b = (R)st->beta;
   R v = 0;
@@ -259,7 +257,6 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? kFp32BlocksPerSM<R> :
   };
   if constexpr (STAGED) stencil_staged<R, 0, MU0, UNIT>(g, k, SrcAxpy<R>{r, p_old, b}, Wt, Wx, epi);
   else stencil_ld<R, 0, MU0, UNIT>(g, k, ld, Wt, Wx, epi);
-  pdl_release();
   double tot;
   if (grid_sum<kBlock, R>(v, red.partials, red.counter, &tot) && threadIdx.x == 0) {
     st->alpha = st->rr / tot;
@@ -278,7 +275,6 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg2_64(Geo g, OpK<double> k, cons
                                                    double2* __restrict__ r, const double2* __restrict__ Wt,
                                                    const double2* __restrict__ Wx, CgState* st, CgLog* log,
                                                    Red red, Cond c, double inv_m2 = 1.0) {
-  pdl_wait();
   if (st->done) return;
   const double a = st->alpha;
   const double ax = UNIT ? a * inv_m2 : a;
@@ -295,7 +291,6 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg2_64(Geo g, OpK<double> k, cons
     v = fma(rv.y, rv.y, v);
   };
   stencil_all<double, 1, MU0, UNIT>(g, k, Mp, Wt, Wx, epi);
-  pdl_release();
   double rn;
   if (grid_sum<kBlock, double>(v, red.partials, red.counter, &rn) && threadIdx.x == 0) {
     st->iter += 1;
@@ -315,47 +310,16 @@ void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const
       g, b, x, w.r, w.p[0], nullptr, rel_tol, abs_tol2, maxiter, 0, log_index, st, log, red, c);
 }
 
-// Launch with a programmatic dependency on the previous kernel of the stream
-// (pdl) or an ordinary one.  The CG kernels call pdl_wait() before they read
-// anything, so both orders are correct; with pdl the next kernel's launch
-// overlaps the previous one's reduction tail.
-template <typename... Exp, typename... Act>
-void launch_k(void (*kernel)(Exp...), int grid, cudaStream_t s, bool pdl, Act&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(kBlock);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = pdl ? 1 : 0;
-  cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
-}
-
-// TG_PDL=1 turns on programmatic dependencies between the FP64 CG kernels.
-// Off by default: at 1024^2 the iteration measured 94.3 us with them against
-// 93.6 us without (the early-launched blocks of the next kernel take SM slots
-// while this one's tail runs).
-bool pdl_enabled() {
-  const char* e = getenv("TG_PDL");
-  return e && e[0] == '1';
-}
-
 void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
-               double2* x, const CgBufs64& w, int half, CgState* st, CgLog* log, const Red& red, Cond c,
-               bool after_kernel) {
+               double2* x, const CgBufs64& w, int half, CgState* st, CgLog* log, const Red& red, Cond c) {
   const int wk = stencil_work(g);
   const double2* p_old = w.p[half];
   double2* p_new = w.p[half ^ 1];
   if (L.Wt1 != nullptr) {
-    const bool pdl = pdl_enabled();
-    TG_OP_DISPATCH(km, launch_k(k_cg1<double, MU0, true>, occ_grid(k_cg1<double, MU0, true>, wk), s,
-                                pdl && after_kernel, g, km, w.r, p_old, p_new, w.Mp, L.Wt1, L.Wx1, st, red));
-    TG_OP_DISPATCH(kd, launch_k(k_cg2_64<MU0, true>, occ_grid(k_cg2_64<MU0, true>, wk), s, pdl, g, kd,
-                                (const double2*)w.Mp, (const double2*)p_new, x, w.r, L.Wt1, L.Wx1, st, log, red,
-                                c, L.inv_m2));
+    TG_OP_DISPATCH(km, (k_cg1<double, MU0, true><<<occ_grid(k_cg1<double, MU0, true>, wk), kBlock, 0, s>>>(
+                            g, km, w.r, p_old, p_new, w.Mp, L.Wt1, L.Wx1, st, red)));
+    TG_OP_DISPATCH(kd, (k_cg2_64<MU0, true><<<occ_grid(k_cg2_64<MU0, true>, wk), kBlock, 0, s>>>(
+                            g, kd, w.Mp, p_new, x, w.r, L.Wt1, L.Wx1, st, log, red, c, L.inv_m2)));
     return;
   }
   TG_OP_DISPATCH(km, (k_cg1<double, MU0><<<occ_grid(k_cg1<double, MU0>, wk), kBlock, 0, s>>>(

@@ -58,11 +58,8 @@ void dslash32(cudaStream_t s, const Geo& g, const OpK<float>& k, int dag, const 
 void cg64_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufs64& w, CgState* st,
                CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int log_index, Cond c);
 // one iteration reading p[half] and writing p[half ^ 1]; iterations alternate half = 0, 1
-// after_kernel: the previous operation of the stream is a kernel, so the first
-// kernel may take a programmatic dependency on it
 void cg64_iter(cudaStream_t s, const Geo& g, const OpK<double>& km, const OpK<double>& kd, const Links& L,
-               double2* x, const CgBufs64& w, int half, CgState* st, CgLog* log, const Red& red, Cond c,
-               bool after_kernel);
+               double2* x, const CgBufs64& w, int half, CgState* st, CgLog* log, const Red& red, Cond c);
 // Mixed precision: FP32 iterations + FP64 reliable update
 void cgmx_init(cudaStream_t s, const Geo& g, const double2* b, double2* x, const CgBufsMixed& w, CgState* st,
                CgLog* log, const Red& red, double rel_tol, double abs_tol2, int maxiter, int ru_interval,
