@@ -382,8 +382,8 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
     g ~ U[0.2, 1.2], 10 leapfrog steps, CG 1e-10): mixed-precision batch in one
     launch per trajectory vs the same chains one at a time on the plain FP64
     single-lattice path (a sample of `sample` chains, scaled)."""
-    from thirring2d_gb300.profile_case import c4_chains
-    chains, fields = c4_chains(nchains)
+    from thirring2d_gb300.profile_case import mixed_size_chains
+    chains, fields = mixed_size_chains(nchains)
     cgm = tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=tg.native.PREC_MIXED, ru_interval=50)
     cg64 = tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=tg.native.PREC_FP64)
 

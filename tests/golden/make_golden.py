@@ -27,11 +27,11 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 
 # name: (nt, nx, m, g, mu, variant, sigma_A, seed, puregauge sweeps, trajectories, nsteps)
 CONFIGS = {
-    # BASELINE C1 shape, reference boundary conditions (x antiperiodic)
+    # the 16^2 workload (m 0.1, g 0.5, 10 steps), reference boundary conditions (x antiperiodic)
     "c1_16x16_apx": (16, 16, 0.1, 0.5, 0.0, "fixed_apx", 0.1, 12345, 10, 3, 10),
-    # BASELINE C1 boundary conditions (x periodic)
+    # the 16^2 workload with a periodic x direction
     "c1_16x16_px": (16, 16, 0.1, 0.5, 0.0, "fixed_px", 0.1, 4242, 10, 3, 10),
-    # C1 shape with a stable step size (40 steps): |dH| < 1, so dH is pinned absolutely
+    # the same with a stable step size (40 steps): |dH| < 1, so dH is pinned absolutely
     "c1s_16x16_px": (16, 16, 0.1, 0.5, 0.0, "fixed_px", 0.1, 2024, 10, 3, 40),
     # chemical potential on: exercises e^{+-mu} and the stochastic-term force
     "mu_8x8_px": (8, 8, 0.3, 0.8, 0.3, "fixed_px", 0.3, 777, 5, 3, 10),

@@ -33,7 +33,7 @@ def lat_args(d: dict):
 
 def dH_ok(got: float, want: float, stable: bool) -> bool:
     """dH parity: 1e-9 absolute where the trajectory is stable (|dH| < 10);
-    relative 1e-9 on the reference's unstable 10-step C1 trajectories, where
+    relative 1e-9 on the reference's unstable 10-step 16^2 trajectories, where
     |dH| reaches 1e5 and the last digits are amplified rounding."""
     if stable:
         return abs(got - want) <= 1e-9

@@ -81,7 +81,7 @@ def test_batch_autotune_keeps_state(tg):
 
 
 def test_batch_mixed_sizes_many_chains(tg):
-    """The C4 shape at reduced count: 64 chains, sides from {16..128}, each with
+    """The batched-chain workload's shape at reduced count: 64 chains, sides from {16..128}, each with
     its own m, g and seed, graph-launched, three trajectories."""
     rng = np.random.default_rng(4)
     sides = [16, 24, 32, 48, 64, 96, 128]

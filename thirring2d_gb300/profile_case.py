@@ -8,6 +8,11 @@ operator applies, then one CG solve capped at `iters` iterations (no
 tolerance, so it runs exactly that many), in the chosen precision, and prints
 the CUDA-event timings.  Numbers printed under a profiler are not benchmark
 values.
+
+Report modes:
+    --batch N [--sequential K]   N chains of mixed sizes in one batched launch
+    --mixed-report --size 2048   FP64 vs mixed-precision solve and trajectories at m 0.02
+    --scaling-report             dH against the leapfrog step at 64^2, two pseudofermions
 """
 from __future__ import annotations
 
@@ -22,7 +27,7 @@ from .lattice import Lattice, cg_params
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--size", type=int, default=1024, help="lattice side (the C3 report uses 2048)")
+    ap.add_argument("--size", type=int, default=1024, help="lattice side (the mixed-precision report uses 2048)")
     ap.add_argument("--iters", type=int, default=100)
     ap.add_argument("--applies", type=int, default=20)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
@@ -30,16 +35,17 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="run the batched-chain case with this many chains")
     ap.add_argument("--trajectories", type=int, default=2)
     ap.add_argument("--sequential", type=int, default=0, help="chains to also run one at a time (FP64 path)")
-    ap.add_argument("--c5", action="store_true", help="the 64^2 differentiation / dH-scaling report")
-    ap.add_argument("--c3", action="store_true", help="the 2048^2 ill-conditioned mixed-precision report")
-    ap.add_argument("--c3-tau", type=float, nargs="+", default=[1.0, 0.05], help="trajectory lengths of the C3 report")
+    ap.add_argument("--scaling-report", action="store_true", help="the 64^2 two-pseudofermion dH-scaling report")
+    ap.add_argument("--mixed-report", action="store_true", help="the ill-conditioned (m 0.02) mixed-precision report")
+    ap.add_argument("--mixed-tau", type=float, nargs="+", default=[1.0, 0.05],
+                    help="trajectory lengths of the mixed-precision report")
     a = ap.parse_args()
     if a.batch:
         return batch_case(a)
-    if a.c5:
-        return c5_case(a)
-    if a.c3:
-        return c3_case(a)
+    if a.scaling_report:
+        return scaling_report(a)
+    if a.mixed_report:
+        return mixed_report(a)
     n = a.size
     rng = np.random.default_rng(n)
     L = Lattice(n, n, 0.05, 0.6, 0.0, N.BC_ANTIPERIODIC, N.BC_PERIODIC)
@@ -61,7 +67,7 @@ def main():
     print(json.dumps(out))
 
 
-def c4_chains(n: int, seed: int = 4):
+def mixed_size_chains(n: int, seed: int = 4):
     """The batched-chain workload: n chains, sides uniform in {16, 24, 32, 48, 64,
     96, 128}, m ~ U[0.05, 0.5], g ~ U[0.2, 1.2], own seeds, A ~ N(0, 0.2^2)."""
     rng = np.random.default_rng(seed)
@@ -79,7 +85,7 @@ def batch_case(a):
     import time
 
     from .lattice import Batch, batch_params, hmc_params
-    chains, fields = c4_chains(a.batch)
+    chains, fields = mixed_size_chains(a.batch)
     B = Batch(chains)
     for i, A in enumerate(fields):
         B.set_gauge(i, A)
@@ -109,7 +115,7 @@ def batch_case(a):
     print(json.dumps(out))
 
 
-def c5_case(a):
+def scaling_report(a):
     """64^2, m 0.1, g 0.5, A ~ N(0, 0.3^2), two pseudofermions: dH statistics over
     a.trajectories trajectories at leapfrog step sizes 0.2, 0.1, 0.05 (and 0.025,
     0.0125 over fewer), FP64 and mixed precision on the same Philox stream."""
@@ -144,7 +150,7 @@ def c5_case(a):
     print(json.dumps(out))
 
 
-def c3_case(a):
+def mixed_report(a):
     """2048^2 (a.size), m 0.02, g 0.8, A ~ N(0, 0.5^2): one CG solve of M^dag M x = b
     to relative residual 1e-10 in FP64 and in FP32 with FP64 reliable updates
     every 50 iterations (iterations, wall time, true residual, distance between
@@ -178,7 +184,7 @@ def c3_case(a):
     # tau 1 is the configuration as specified (30 steps of 1/30: the MD is
     # unstable there, |dH| ~ 1e12); tau 0.05 (30 steps of 1/600) is a step
     # size at which it is stable, so the dH difference measures the solver
-    for tau in a.c3_tau:
+    for tau in a.mixed_tau:
         runs = {}
         for prec, name in ((N.PREC_FP64, "fp64"), (N.PREC_MIXED, "mixed")):
             L = Lattice(n, n, m, g, 0.0, N.BC_ANTIPERIODIC, N.BC_PERIODIC)
