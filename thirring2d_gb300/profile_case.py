@@ -35,6 +35,8 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="run the batched-chain case with this many chains")
     ap.add_argument("--trajectories", type=int, default=2)
     ap.add_argument("--sequential", type=int, default=0, help="chains to also run one at a time (FP64 path)")
+    ap.add_argument("--ru-interval", type=int, default=50, help="mixed precision: iterations between reliable updates")
+    ap.add_argument("--side", type=int, default=0, help="batched case: give every chain this side")
     ap.add_argument("--scaling-report", action="store_true", help="the 64^2 two-pseudofermion dH-scaling report")
     ap.add_argument("--mixed-report", action="store_true", help="the ill-conditioned (m 0.02) mixed-precision report")
     ap.add_argument("--mixed-tau", type=float, nargs="+", default=[1.0, 0.05],
@@ -67,11 +69,12 @@ def main():
     print(json.dumps(out))
 
 
-def mixed_size_chains(n: int, seed: int = 4):
+def mixed_size_chains(n: int, seed: int = 4, side: int = 0):
     """The batched-chain workload: n chains, sides uniform in {16, 24, 32, 48, 64,
-    96, 128}, m ~ U[0.05, 0.5], g ~ U[0.2, 1.2], own seeds, A ~ N(0, 0.2^2)."""
+    96, 128} (or all `side`), m ~ U[0.05, 0.5], g ~ U[0.2, 1.2], own seeds,
+    A ~ N(0, 0.2^2)."""
     rng = np.random.default_rng(seed)
-    sides = np.array([16, 24, 32, 48, 64, 96, 128])
+    sides = np.array([side] if side else [16, 24, 32, 48, 64, 96, 128])
     chains, fields = [], []
     for k in range(n):
         L = int(rng.choice(sides))
@@ -85,13 +88,13 @@ def batch_case(a):
     import time
 
     from .lattice import Batch, batch_params, hmc_params
-    chains, fields = mixed_size_chains(a.batch)
+    chains, fields = mixed_size_chains(a.batch, side=a.side)
     B = Batch(chains)
     for i, A in enumerate(fields):
         B.set_gauge(i, A)
     prec = N.PREC_MIXED if a.precision == "mixed" else N.PREC_FP64
     bp = batch_params(nsteps=10, use_graph=bool(a.graph),
-                      cg=cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=prec, ru_interval=50))
+                      cg=cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=prec, ru_interval=a.ru_interval))
     block, tune_ms = B.autotune(bp)
     out = {"chains": a.batch, "sites": B.total_sites(), "precision": a.precision, "block": block,
            "tune_ms": tune_ms, "traj_ms": []}
@@ -101,6 +104,9 @@ def batch_case(a):
         out["status"] = max(r.status for r in res)
         out["acceptance"] = float(np.mean([r.accepted for r in res]))
         out["cg_iterations_mean"] = float(np.mean([r.cg_iterations for r in res]))
+        out["cg_iterations_max"] = int(max(r.cg_iterations for r in res))
+        out["reliable_updates_mean"] = float(np.mean([r.reliable_updates for r in res]))
+        out["dH"] = [r.dH for r in res[:8]]
     B.close()
     if a.sequential:
         cg64 = cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=N.PREC_FP64)
