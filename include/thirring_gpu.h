@@ -273,8 +273,10 @@ int tg_cg_noalloc(const tg_lattice_params* p, const tg_cg_params* cp, const void
 
 /* ---- batched chains ------------------------------------------------------
  * Many independent HMC chains (different NT x NX, m, g, mu, seed) advanced
- * by one persistent kernel launch per trajectory: each thread block runs whole
- * chain trajectories (hmc.c:671-746) taken from a work queue, largest first.
+ * by one persistent kernel launch per trajectory: each team -- one thread
+ * block, or a thread-block cluster of 2 or 4 blocks on as many SMs -- runs
+ * whole chain trajectories (hmc.c:671-746) taken from a work queue, largest
+ * first.
  * The reference runs one chain per process; a batch replaces N such runs.
  * Random fields are the Philox streams of TG_RNG_PHILOX keyed by each chain's
  * seed, so chain k reproduces a tg_lattice trajectory with the same seed. */
@@ -292,7 +294,11 @@ typedef struct {
   double tau;               /* trajectory length                               */
   int stochastic_term;      /* as tg_hmc_params                                */
   int use_graph;            /* launch through a cached CUDA graph              */
-  int block;                /* threads per block: 128, 256, 384 or 512; 0 = the tuned kernel instance */
+  int block;                /* kernel instance: 0 = the tuned one; 128, 256, 384 or 512 threads
+                               per block (one block per chain); or an instance id as
+                               tg_batch_autotune reports it (block * 100 + 10 * blocks
+                               per chain, when a thread-block cluster of 2 or 4 blocks
+                               runs each chain, + minimum resident blocks per SM)   */
   tg_cg_params cg;          /* per-chain solver                                */
 } tg_batch_params;
 
@@ -308,10 +314,11 @@ int tg_batch_get_gauge(tg_batch* B, int chain, double* A);
 int tg_batch_trajectory(tg_batch* B, const tg_batch_params* p, tg_traj_result* results);
 /* Times one trajectory with every compiled instance of the batch kernel
  * (threads per block x minimum resident blocks per SM, which trades registers
- * against occupancy), with the chains' state saved and restored around every
- * trial, and makes the fastest the default (p->block = 0).
- * *best_block = 100 * threads + blocks per SM of the winner; *best_ms = its
- * device time. */
+ * against occupancy, and one block or a cluster of 2 or 4 blocks per chain),
+ * with the chains' state saved and restored around every trial, and makes the
+ * fastest the default (p->block = 0).  *best_block = the winner's instance id
+ * (100 * threads + 10 * blocks per chain if clustered + blocks per SM);
+ * *best_ms = its device time. */
 int tg_batch_autotune(tg_batch* B, const tg_batch_params* p, int* best_block, double* best_ms);
 
 #ifdef __cplusplus

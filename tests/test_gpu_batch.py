@@ -99,3 +99,44 @@ def test_batch_mixed_sizes_many_chains(tg):
         if prev is not None:
             assert any(a.Spf0 != b.Spf0 for a, b in zip(prev, res))   # fresh fields each trajectory
         prev = res
+
+
+@pytest.mark.parametrize("instance", [51221, 51241, 25641])
+def test_cluster_instances_match_block_instance(tg, instance):
+    """Chains split over thread-block clusters (2 or 4 blocks, distributed
+    shared memory sums) against one block per chain: the same trajectories to
+    the rounding of the team sums."""
+    from thirring2d_gb300.profile_case import mixed_size_chains
+    chains, fields = mixed_size_chains(24, seed=9)
+    runs = {}
+    for inst in (51201, instance):
+        B = tg.Batch(chains)
+        for i, A in enumerate(fields):
+            B.set_gauge(i, A)
+        bp = tg.batch_params(nsteps=10, block=inst,
+                             cg=tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=1, ru_interval=50))
+        runs[inst] = [B.trajectory(bp) for _ in range(2)]
+        runs[inst, "A"] = [B.get_gauge(i) for i in range(len(chains))]
+        B.close()
+    # Chains whose MD is unstable at this step size (|dH| ~ 1e6) amplify the
+    # different rounding of the team sums chaotically: for them only the
+    # outcome is compared (both far from 0, the same decision); the stable
+    # ones tightly.
+    same = np.ones(len(chains), bool)   # the chain's state is still the same in both runs
+    tight = 0
+    for ta, tb in zip(runs[51201], runs[instance]):
+        for k, (a, b) in enumerate(zip(ta, tb)):
+            assert a.status == 0 and b.status == 0
+            if not same[k]:
+                continue
+            assert abs(a.Spf0 - b.Spf0) <= 1e-12 * abs(a.Spf0)      # same Philox fields
+            if abs(a.dH) < 50:
+                assert abs(a.dH - b.dH) < 1e-6, (k, a.dH, b.dH)
+                assert a.accepted == b.accepted
+                tight += 1
+            else:
+                assert np.isfinite(b.dH) and abs(b.dH) > 10 and a.accepted == b.accepted, (k, a.dH, b.dH)
+                same[k] = not a.accepted      # a rejected trajectory leaves A as it was
+    assert tight >= 8
+    for k in np.where(same)[0]:
+        assert np.abs(runs[51201, "A"][k] - runs[instance, "A"][k]).max() < 1e-8

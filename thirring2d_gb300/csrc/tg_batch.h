@@ -42,16 +42,25 @@ struct ChainResult {
   unsigned long long traj;
 };
 
-// kernel instances of the batched trajectory: threads per block, min blocks per SM
+// kernel instances of the batched trajectory: threads per block, min blocks per
+// SM, and blocks per chain (1: one block per chain; > 1: a thread-block cluster)
 struct BatchCfg {
-  int block, minb;
+  int block, minb, cluster;
 };
-constexpr int kBatchNumCfgs = 6;
+constexpr int kBatchNumCfgs = 9;
 extern const BatchCfg kBatchCfgs[kBatchNumCfgs];
 
-void batch_trajectory(cudaStream_t s, int cfg, int grid, const BatchChain* chains, const int* order, int n,
+// Launches instance cfg over n chains with as many teams as can be resident.
+void batch_trajectory(cudaStream_t s, int cfg, int sms, const BatchChain* chains, const int* order, int n,
                       const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue);
-// resident blocks per SM of kernel instance cfg (0 if it cannot launch)
-int batch_blocks_per_sm(int cfg);
+// teams (blocks or clusters) of instance cfg that can be resident at once (0: cannot launch)
+int batch_teams(int cfg, int sms);
+// the tuned instance as reported to callers: block * 100 + 10 * cluster (if > 1) + min blocks per SM
+inline int batch_cfg_id(const BatchCfg& c) { return c.block * 100 + (c.cluster > 1 ? 10 * c.cluster : 0) + c.minb; }
+
+// tg_batch_cluster.cu: instance `which` (0: 512 x 2 blocks, 1: 512 x 4, 2: 256 x 4)
+int batch_cluster_max(int which);
+void batch_cluster_launch(cudaStream_t s, int which, int clusters, const BatchChain* chains, const int* order, int n,
+                          const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue);
 
 }  // namespace tg

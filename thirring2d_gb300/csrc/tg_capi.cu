@@ -1362,27 +1362,28 @@ struct tg_batch {
 
 namespace {
 
-// kernel instance for p.block: the tuned one, else the instance with that
-// block size and the most resident blocks per SM
+// kernel instance for p.block: 0 the tuned one; a block size the first
+// one-block-per-chain instance with that size; an instance id as
+// tg_batch_autotune reports it that instance
 int batch_cfg(const tg_batch* B, const tg_batch_params& p) {
   if (p.block <= 0) return B->tuned_cfg;
+  for (int c = 0; c < kBatchNumCfgs; c++)
+    if (batch_cfg_id(kBatchCfgs[c]) == p.block) return c;
   for (int c = 0; c < kBatchNumCfgs; c++)
     if (kBatchCfgs[c].block == p.block) return c;
   return -1;
 }
 
 int batch_launch(tg_batch* B, const tg_batch_params& p, int cfg, cudaStream_t s) {
-  if (cfg < 0 || cfg >= kBatchNumCfgs) return fail(TG_E_ARG, "block must be 0, 128, 256, 384 or 512");
-  int per_sm = batch_blocks_per_sm(cfg);
-  if (per_sm <= 0) return fail(TG_E_CUDA, "batch kernel cannot launch at this block size");
-  int grid = std::min(B->n, per_sm * B->sms);
+  if (cfg < 0 || cfg >= kBatchNumCfgs) return fail(TG_E_ARG, "unknown batch kernel instance");
+  if (batch_teams(cfg, B->sms) <= 0) return fail(TG_E_CUDA, "batch kernel instance cannot launch on this GPU");
   BatchTraj t;
   t.nsteps = p.nsteps;
   t.tau = p.tau;
   t.stochastic_term = p.stochastic_term;
   t.cg = BatchCg{p.cg.rel_tol, p.cg.abs_tol2, p.cg.maxiter, p.cg.precision, p.cg.ru_interval};
   TG_CK(cudaMemsetAsync(B->d_queue, 0, sizeof(unsigned), s));
-  batch_trajectory(s, cfg, grid, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
+  batch_trajectory(s, cfg, B->sms, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
   TG_CK(cudaGetLastError());
   return TG_OK;
 }
@@ -1425,8 +1426,10 @@ int batch_run(tg_batch* B, const tg_batch_params& p, int cfg, double* ms) {
 int check_batch_params(const tg_batch_params* p) {
   if (!p) return fail(TG_E_ARG, "null batch parameters");
   if (p->nsteps <= 0 || !(p->tau > 0)) return fail(TG_E_ARG, "nsteps and tau must be positive");
-  if (p->block != 0 && p->block != 128 && p->block != 256 && p->block != 384 && p->block != 512)
-    return fail(TG_E_ARG, "block must be 0, 128, 256, 384 or 512");
+  bool known = p->block == 0;
+  for (int c = 0; c < kBatchNumCfgs && !known; c++)
+    known = p->block == kBatchCfgs[c].block || p->block == batch_cfg_id(kBatchCfgs[c]);
+  if (!known) return fail(TG_E_ARG, "block must be 0, a block size (128, 256, 384, 512) or an instance id");
   return check_cg_params(&p->cg);
 }
 
@@ -1598,7 +1601,7 @@ int tg_batch_autotune(tg_batch* B, const tg_batch_params* p, int* best_block, do
   int best = -1;
   double bms = 1e300;
   for (int c = 0; c < kBatchNumCfgs; c++) {
-    if (batch_blocks_per_sm(c) <= 0) continue;
+    if (batch_teams(c, B->sms) <= 0) continue;
     double ms = 0;
     tg_batch_params q = *p;
     q.use_graph = 0;
@@ -1615,7 +1618,7 @@ int tg_batch_autotune(tg_batch* B, const tg_batch_params* p, int* best_block, do
   cleanup();
   if (best < 0) return fail(TG_E_CUDA, "no kernel instance could run the batch");
   B->tuned_cfg = best;
-  if (best_block) *best_block = kBatchCfgs[best].block * 100 + kBatchCfgs[best].minb;
+  if (best_block) *best_block = batch_cfg_id(kBatchCfgs[best]);
   if (best_ms) *best_ms = bms;
   return TG_OK;
 }

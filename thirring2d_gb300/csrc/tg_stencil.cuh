@@ -136,15 +136,18 @@ __device__ __forceinline__ void stencil_all(const Geo& g, const OpK<R>& k, const
   stencil_ld<R, DAG, MU0, UNIT>(g, k, ld, Wt, Wx, epi);
 }
 
-// The operator over one small lattice inside one thread block (the batched-chain
-// kernel): the block's warps split the lattice's (strip, t) rows into one
-// contiguous range each, as for_warp_rows splits them over a grid; lattices
-// whose nx is not a multiple of 32 go one site per thread.
-template <typename R, int DAG, bool MU0, class Ld, class Epi>
-__device__ __forceinline__ void stencil_block(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
-                                              const C2<R>* __restrict__ Wx, Epi& epi) {
+// The operator over one small lattice run by a team of thread blocks (the
+// batched-chain kernel: one block, or the blocks of a cluster).  T gives the
+// block's rank in the team and the team's size.  The team's warps split the
+// lattice's (strip, t) rows into one contiguous range each, as for_warp_rows
+// splits them over a grid; lattices whose nx is not a multiple of 32 go one
+// site per thread.
+template <class T, typename R, int DAG, bool MU0, class Ld, class Epi>
+__device__ __forceinline__ void stencil_team(const Geo& g, const OpK<R>& k, Ld& ld, const C2<R>* __restrict__ Wt,
+                                             const C2<R>* __restrict__ Wx, Epi& epi) {
+  const int wpb = blockDim.x >> 5;
   if ((g.nx & 31) == 0) {
-    const int nw = blockDim.x >> 5, w = threadIdx.x >> 5;
+    const int nw = T::nblocks() * wpb, w = T::rank() * wpb + (threadIdx.x >> 5);
     const int rows = (g.nx >> 5) * g.nt;
     int r = (int)((long long)rows * w / nw);
     const int r1 = (int)((long long)rows * (w + 1) / nw);
@@ -156,7 +159,7 @@ __device__ __forceinline__ void stencil_block(const Geo& g, const OpK<R>& k, Ld&
       r += tb - ta;
     }
   } else {
-    for (int s = threadIdx.x; s < g.V; s += blockDim.x) {
+    for (int s = T::rank() * (int)blockDim.x + (int)threadIdx.x; s < g.V; s += T::nblocks() * (int)blockDim.x) {
       int t, x;
       site_tx(g, s, t, x);
       const Nbr n = neighbours(g, s, t, x);
