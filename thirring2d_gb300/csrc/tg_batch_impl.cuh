@@ -348,7 +348,8 @@ __device__ void chain_trajectory(const ChainCtx& c, const BatchTraj& P, ChainRes
     TG_BSITES(s, V) c.Mx[s] = dslash_at<double, 0, MU0>(g, km, c.x, c.Wt, c.Wx, s);
     T::sync();
     TG_BSITES(s, V) {
-      ForcePieces f = force_site(g, c.ep, c.em, c.An, c.Wt, c.Wx, c.x, c.Mx, noise_on ? c.noise : nullptr, s);
+      ForcePieces f = force_site(g, c.bc_t, c.bc_x, c.ep, c.em, c.An, c.Wt, c.Wx, c.x, c.Mx,
+                                 noise_on ? c.noise : nullptr, s);
       double2 p = c.mom[s];
       p.x -= gfac * f.g.x;
       p.y -= gfac * f.g.y;

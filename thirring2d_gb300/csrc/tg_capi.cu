@@ -544,13 +544,13 @@ int enqueue_trajectory(tg_lattice* L, cudaStream_t s, const tg_hmc_params& p, bo
   for (int i = 0; i < p.nsteps; i++) {
     gauge_step(s, g, L->P.bc_t, L->P.bc_x, L->Anew, L->mom, c, i == 0 ? 1 : 2, link_out(L));
     if (p.npf == 0)
-      momentum_update(s, g, ep, em, L->Anew, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->mom, eps, gfac,
+      momentum_update(s, g, L->P.bc_t, L->P.bc_x, ep, em, L->Anew, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->mom, eps, gfac,
                       1 | (use_noise ? 2 : 0));
     for (int k = 0; k < p.npf; k++) {
       TG_TRY(cg(L->phi + (size_t)k * V, L->chi));
       dslash64(s, g, km, 0, L->chi, L->Mchi, L->Wt, L->Wx);
       int flags = (k == 0 ? 1 : 0) | ((k == p.npf - 1 && use_noise) ? 2 : 0);
-      momentum_update(s, g, ep, em, L->Anew, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->mom, eps, gfac, flags);
+      momentum_update(s, g, L->P.bc_t, L->P.bc_x, ep, em, L->Anew, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->mom, eps, gfac, flags);
     }
   }
   gauge_step(s, g, L->P.bc_t, L->P.bc_x, L->Anew, L->mom, c, 1, link_out(L));
@@ -934,13 +934,13 @@ int tg_force(tg_lattice* L, int npf, const double* chi, const double* noise, dou
   TG_CK(cudaMemsetAsync(L->vout, 0, V * sizeof(double2), L->stream));  // F accumulates in vout
   if (noise) TG_TRY(upload(L, L->noise, noise, 2 * V));
   if (npf == 0)
-    force_field(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->vout, kNf / L->P.g,
+    force_field(L->stream, L->g, L->P.bc_t, L->P.bc_x, ep, em, L->A, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->vout, kNf / L->P.g,
                 1 | (noise ? 2 : 0));
   for (int k = 0; k < npf; k++) {
     TG_TRY(upload(L, L->chi, chi + 2 * V * k, 2 * V));
     dslash64(L->stream, L->g, op_k(L, 0), 0, L->chi, L->Mchi, L->Wt, L->Wx);
     int flags = (k == 0 ? 1 : 0) | ((k == npf - 1 && noise) ? 2 : 0);
-    force_field(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->vout, kNf / L->P.g,
+    force_field(L->stream, L->g, L->P.bc_t, L->P.bc_x, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->vout, kNf / L->P.g,
                 flags);
   }
   TG_CK(cudaGetLastError());
@@ -965,7 +965,7 @@ int tg_pf_force(tg_lattice* L, const tg_cg_params* cp, int npf, const double* ph
     acc.rr = r.rr;
     acc.rr0 = r.rr0;
     dslash64(L->stream, L->g, op_k(L, 0), 0, L->chi, L->Mchi, L->Wt, L->Wx);
-    force_field(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, nullptr, L->vout, 0.0, 0);
+    force_field(L->stream, L->g, L->P.bc_t, L->P.bc_x, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, nullptr, L->vout, 0.0, 0);
   }
   TG_CK(cudaGetLastError());
   if (res) *res = acc;
@@ -986,7 +986,7 @@ int tg_momentum_step(tg_lattice* L, const tg_cg_params* cp, double* mom, int npf
   if (npf > 0) TG_TRY(upload(L, L->phi, phi, 2 * V * npf));
   tg_cg_result acc{};
   if (npf == 0)
-    momentum_update(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->mom, eps, gfac,
+    momentum_update(L->stream, L->g, L->P.bc_t, L->P.bc_x, ep, em, L->A, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->mom, eps, gfac,
                     1 | (noise ? 2 : 0));
   for (int k = 0; k < npf; k++) {
     tg_cg_result r{};
@@ -998,7 +998,7 @@ int tg_momentum_step(tg_lattice* L, const tg_cg_params* cp, double* mom, int npf
     acc.rr0 = r.rr0;
     dslash64(L->stream, L->g, op_k(L, 0), 0, L->chi, L->Mchi, L->Wt, L->Wx);
     int flags = (k == 0 ? 1 : 0) | ((k == npf - 1 && noise) ? 2 : 0);
-    momentum_update(L->stream, L->g, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->mom, eps, gfac,
+    momentum_update(L->stream, L->g, L->P.bc_t, L->P.bc_x, ep, em, L->A, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->mom, eps, gfac,
                     flags);
   }
   TG_CK(cudaGetLastError());

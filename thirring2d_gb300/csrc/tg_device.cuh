@@ -123,15 +123,22 @@ struct ForcePieces {
   double2 g, pf, md;
 };
 
-__device__ __forceinline__ ForcePieces force_site(const Geo& g, double ep, double em, const double2* A,
-                                                  const double2* Wt, const double2* Wx, const double2* chi,
-                                                  const double2* Mchi, const double2* noise, int s) {
+// The gauge force's sin A comes from the link coefficient the same gauge step
+// wrote: W = f e^{iA} with f = +-1/2, so sin A = Im W / f exactly (f and 1/f
+// are powers of two).  A link with f = 0 (open boundary) takes sin A itself.
+__device__ __forceinline__ ForcePieces force_site(const Geo& g, int bc_t, int bc_x, double ep, double em,
+                                                  const double2* A, const double2* Wt, const double2* Wx,
+                                                  const double2* chi, const double2* Mchi, const double2* noise,
+                                                  int s) {
   int t, x;
   site_tx(g, s, t, x);
   Nbr n = neighbours(g, s, t, x);
   ForcePieces f;
-  double2 a = A[s];
-  f.g = make_double2(sin(a.x), sin(a.y));
+  const double bt = (t == g.nt - 1) ? (double)bc_t : 1.0;
+  const double bx = (x == g.nx - 1) ? (double)bc_x : 1.0;
+  const double inv_ft = ((x & 1) ? -2.0 : 2.0) * bt, inv_fx = 2.0 * bx;
+  f.g.x = (bt != 0.0) ? Wt[s].y * inv_ft : sin(A[s].x);
+  f.g.y = (bx != 0.0) ? Wx[s].y * inv_fx : sin(A[s].y);
   f.pf = make_double2(0, 0);
   f.md = make_double2(0, 0);
   if (chi != nullptr) {

@@ -534,7 +534,8 @@ void md_action(cudaStream_t s, const Geo& g, const OpK<double>& kd, const double
 // with e^{+-mu} on t links only.  The three parts are subtracted from p in
 // the reference's order.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_momentum_update(Geo g, double ep, double em, const double2* __restrict__ A,
+__global__ void __launch_bounds__(kBlock) k_momentum_update(Geo g, int bc_t, int bc_x, double ep, double em,
+                                                            const double2* __restrict__ A,
                                                             const double2* __restrict__ Wt,
                                                             const double2* __restrict__ Wx,
                                                             const double2* __restrict__ chi,
@@ -542,7 +543,7 @@ __global__ void __launch_bounds__(kBlock) k_momentum_update(Geo g, double ep, do
                                                             const double2* __restrict__ noise, double2* mom,
                                                             double eps, double gfac, int flags) {
   TG_SITES(s, g.V) {
-    ForcePieces f = force_site(g, ep, em, A, Wt, Wx, chi, Mchi, (flags & 2) ? noise : nullptr, s);
+    ForcePieces f = force_site(g, bc_t, bc_x, ep, em, A, Wt, Wx, chi, Mchi, (flags & 2) ? noise : nullptr, s);
     double2 p = mom[s];
     if (flags & 1) {
       p.x -= gfac * f.g.x;
@@ -560,14 +561,15 @@ __global__ void __launch_bounds__(kBlock) k_momentum_update(Geo g, double ep, do
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_force_field(Geo g, double ep, double em, const double2* __restrict__ A,
+__global__ void __launch_bounds__(kBlock) k_force_field(Geo g, int bc_t, int bc_x, double ep, double em,
+                                                        const double2* __restrict__ A,
                                                         const double2* __restrict__ Wt, const double2* __restrict__ Wx,
                                                         const double2* __restrict__ chi,
                                                         const double2* __restrict__ Mchi,
                                                         const double2* __restrict__ noise, double2* F, double gfac,
                                                         int flags) {
   TG_SITES(s, g.V) {
-    ForcePieces f = force_site(g, ep, em, A, Wt, Wx, chi, Mchi, (flags & 2) ? noise : nullptr, s);
+    ForcePieces f = force_site(g, bc_t, bc_x, ep, em, A, Wt, Wx, chi, Mchi, (flags & 2) ? noise : nullptr, s);
     double2 o = F[s];
     if (flags & 1) {
       o.x += gfac * f.g.x;
@@ -579,15 +581,17 @@ __global__ void __launch_bounds__(kBlock) k_force_field(Geo g, double ep, double
   }
 }
 
-void momentum_update(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
-                     const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise,
-                     double2* mom, double eps, double gfac, int flags) {
-  k_momentum_update<<<stream_grid(g.V), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, mom, eps, gfac, flags);
+void momentum_update(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double ep, double em, const double2* A,
+                     const double2* Wt, const double2* Wx, const double2* chi, const double2* Mchi,
+                     const double2* noise, double2* mom, double eps, double gfac, int flags) {
+  k_momentum_update<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, ep, em, A, Wt, Wx, chi, Mchi, noise, mom, eps,
+                                                        gfac, flags);
 }
-void force_field(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
-                 const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise, double2* F,
-                 double gfac, int flags) {
-  k_force_field<<<stream_grid(g.V), kBlock, 0, s>>>(g, ep, em, A, Wt, Wx, chi, Mchi, noise, F, gfac, flags);
+void force_field(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double ep, double em, const double2* A,
+                 const double2* Wt, const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise,
+                 double2* F, double gfac, int flags) {
+  k_force_field<<<stream_grid(g.V), kBlock, 0, s>>>(g, bc_t, bc_x, ep, em, A, Wt, Wx, chi, Mchi, noise, F, gfac,
+                                                    flags);
 }
 
 // ---------------------------------------------------------------------------

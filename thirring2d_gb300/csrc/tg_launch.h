@@ -79,13 +79,14 @@ void md_action(cudaStream_t s, const Geo& g, const OpK<double>& kd, const double
                const double2* Wx, double* dst, const Red& red);
 
 // mom -= eps*F; flags bit0: gauge force first (gfac = eps*Nf/g), bit1: stochastic-term force last
-void momentum_update(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
-                     const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise,
-                     double2* mom, double eps, double gfac, int flags);
+// (bc_t, bc_x: the lattice's boundary conditions, which the link coefficients carry)
+void momentum_update(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double ep, double em, const double2* A,
+                     const double2* Wt, const double2* Wx, const double2* chi, const double2* Mchi,
+                     const double2* noise, double2* mom, double eps, double gfac, int flags);
 // F = dS/dA (for tests): same pieces, written instead of applied
-void force_field(cudaStream_t s, const Geo& g, double ep, double em, const double2* A, const double2* Wt,
-                 const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise, double2* F,
-                 double gfac, int flags);
+void force_field(cudaStream_t s, const Geo& g, int bc_t, int bc_x, double ep, double em, const double2* A,
+                 const double2* Wt, const double2* Wx, const double2* chi, const double2* Mchi, const double2* noise,
+                 double2* F, double gfac, int flags);
 
 // Philox Gaussian fields: out[n] complex pairs for (seed, stats->traj, stream_id)
 void philox_gauss(cudaStream_t s, const Geo& g, unsigned long long seed, const TrajStats* ts, unsigned stream_id,
