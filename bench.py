@@ -435,8 +435,11 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
             "sequential_fp64": {"value": seq_rate, "unit": "chain-trajectories/s",
                                 "sample": f"{sample} of the {nchains} chains, one at a time, second trajectory each"},
             "speedup_vs_sequential_fp64": batched_rate / seq_rate,
-            "dH_rel_err_vs_fp64_batch_max": dh_err, "accept_mismatch_vs_fp64": acc_mismatch,
-            "stable_chains": len(stable), "dH_abs_err_vs_fp64_stable_chains_max": dh_err_stable,
+            "dH_vs_fp64_batch": {
+                "stable_chains": len(stable), "max_abs_err_stable_chains": dh_err_stable,
+                "max_rel_err_all_chains": dh_err, "accept_mismatch": acc_mismatch,
+                "note": "chains with |dH| >= 5 have unstable MD at this step size, where dH differs "
+                        "chaotically between precisions; the decisions still agree"},
             "acceptance": float(np.mean([r.accepted for r in res[-1]])),
             "cg_iterations_per_chain_traj": float(np.mean([r.cg_iterations for r in res[-1]]))}
 
