@@ -197,6 +197,53 @@ def cpu_sample(repeats: int = 3):
                 sec_per_cg_iter=t_iter, sec_per_apply=t_apply)
 
 
+def _ref_cg_rate(job):
+    """Site-iterations/s of the reference's fmdm_invert_cg on one host core
+    (oracle/_ref sample build: 20 iterations per call) at side x side, counted
+    over about `seconds`; the oracle restatement where that build is absent."""
+    side, seconds, seed = job
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    A = rng.normal(0, 0.2, (side, side, 2))
+    b = rng.normal(size=(side, side)) + 1j * rng.normal(size=(side, side))
+    if O.ref_available(side, side, "sample_px"):
+        ref = O.RefHMC(side, side, 0.2, 0.6, 0.0, warmup=0, variant="sample_px")
+        ref.set_A(A)
+        kind, step = "reference", (lambda: ref.cg(b))
+    else:
+        o = O.Oracle(side, side, 0.2, 0.6, 0.0, -1, 1)
+        kind, step = "port", (lambda: o.cg(A, b, rel_tol=0, abs_tol2=0, maxiter=20))
+    step()
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        step()
+        n += 1
+    return side * side * 20 * n / (time.perf_counter() - t0), kind
+
+
+def cpu_batch_sample(chains, iterations, seconds: float = 4.0):
+    """The batched workload on the host: one reference process per core, as
+    independent chains would run there.  Every core runs the reference CG at
+    16x16 (half of the cores) or 64x64 (the other half) at the same time; a
+    chain's trajectory costs V * (its CG iterations + 13 applies / 2) site-
+    iterations at the per-core rate of the nearer sampled size (sides <= 32:
+    16x16, larger: 64x64), and the cores share the chains."""
+    import multiprocessing as mp
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    jobs = [(16 if k % 2 == 0 else 64, seconds, 1000 + k) for k in range(cores)]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        out = pool.map(_ref_cg_rate, jobs)
+    rate = {side: statistics.mean(r for (sd, _, _), (r, _) in zip(jobs, out) if sd == side) for side in (16, 64)}
+    kind = out[0][1]
+    work_s = sum(c["nt"] * c["nx"] * (it + 13 / 2) / rate[16 if c["nt"] <= 32 else 64]
+                 for c, it in zip(chains, iterations))                   # core-seconds per batch trajectory
+    return {"value": len(chains) * cores / work_s, "unit": "chain-trajectories/s", "cores": cores, "kind": kind,
+            "sec_per_site_iteration": {str(k): 1.0 / v for k, v in rate.items()},
+            "sample": f"{cores} concurrent processes, each {seconds:.0f} s of the reference CG (20 iterations per "
+                      f"call) at 16x16 or 64x64; scaled by each chain's FP64 CG iterations of one batch "
+                      f"trajectory plus 13 applies"}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -402,6 +449,7 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
     # chains whose MD is stable at this step size (|dH| < 5): the absolute dH error there
     stable = [(a, b) for a, b in zip(first_m, first_64) if abs(b.dH) < 5.0]
     dh_err_stable = max((abs(a.dH - b.dH) for a, b in stable), default=0.0)
+    iters64 = [r.cg_iterations for r in first_64]
     B64.close()
     steps = max(1, args.steps)
     ms = 0.0
@@ -429,12 +477,14 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
         L.close()
     seq_rate = sample / (seq_ms / 1e3)
     Bm.close()
+    cpu = cpu_batch_sample(chains, iters64)
     return {"value": batched_rate, "unit": "chain-trajectories/s", "chains": nchains,
             "sites": int(sum(c["nt"] * c["nx"] for c in chains)), "precision": "mixed (FP32 CG + FP64 reliable updates)",
             "kernel_instance": cfg, "ms_per_batch_trajectory": ms / steps,
             "sequential_fp64": {"value": seq_rate, "unit": "chain-trajectories/s",
                                 "sample": f"{sample} of the {nchains} chains, one at a time, second trajectory each"},
             "speedup_vs_sequential_fp64": batched_rate / seq_rate,
+            "cpu_reference": cpu,
             "dH_vs_fp64_batch": {
                 "stable_chains": len(stable), "max_abs_err_stable_chains": dh_err_stable,
                 "max_rel_err_all_chains": dh_err, "accept_mismatch": acc_mismatch,

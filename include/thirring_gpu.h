@@ -180,6 +180,23 @@ int tg_puregauge_sweeps(tg_lattice* L, int sweeps);
  * dir inner) the proposal uniform then the acceptance uniform. */
 int tg_puregauge_ext(tg_lattice* L, const double* u, int sweeps);
 
+/* ---- checkpoint and resume ------------------------------------------------
+ * hmc.c keeps no state between runs (fermionbag.c:125-163 writes its raw
+ * field).  A checkpoint holds everything a resumed run needs to continue
+ * bitwise: couplings, the reference MT stream (words and pending outputs),
+ * the Philox trajectory counter and A.  Little-endian layout, byte offsets:
+ *   0  char[8] "TGCKPT01"      8  int32 version (1)     12 int32 nt
+ *   16 int32 nx                20 int32 bc_t            24 int32 bc_x
+ *   28 int32 MT outputs left   32 int32 MT seeded       36 int32 (0)
+ *   40 double m                48 double g              56 double mu
+ *   64 uint64 Philox trajectory counter
+ *   72 uint32[624] MT words    2568 double[624] MT outputs of the current block
+ *   7560 double[nt*nx*2] A ([t][x][dir], as tg_set_gauge).
+ * Loading needs a lattice of the same nt, nx and boundary conditions. */
+size_t tg_checkpoint_size(const tg_lattice* L);
+int tg_checkpoint_save(tg_lattice* L, void* buf, size_t size);
+int tg_checkpoint_load(tg_lattice* L, const void* buf, size_t size);
+
 /* ---- HMC trajectory: update_gauge (hmc.c:671-746) ------------------------- */
 /* Draws the pseudofermion, momentum, noise fields and the accept uniform
  * from the stream p->rng selects (TG_RNG_MT: the reference's order, so the

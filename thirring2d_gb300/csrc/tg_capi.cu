@@ -1024,6 +1024,79 @@ int tg_mt_seed(tg_lattice* L, long seed, long warmup) {
   return TG_OK;
 }
 
+// ---- checkpoint -------------------------------------------------------------
+// Layout (little-endian, as the host stores it): a fixed header, the MT
+// stream's words, its pending outputs, then A.  Offsets in bytes.
+namespace {
+constexpr char kCkptMagic[8] = {'T', 'G', 'C', 'K', 'P', 'T', '0', '1'};
+struct CkptHeader {                 // 72 bytes
+  char magic[8];
+  int32_t version, nt, nx, bc_t, bc_x, mt_avail, mt_seeded, pad_;
+  double m, g, mu;
+  uint64_t traj;                    // Philox trajectory counter
+};
+size_t ckpt_bytes(const tg_lattice* L) {
+  return sizeof(CkptHeader) + 624 * sizeof(uint32_t) + 624 * sizeof(double) + 2 * (size_t)L->V * sizeof(double);
+}
+}  // namespace
+
+size_t tg_checkpoint_size(const tg_lattice* L) { return L ? ckpt_bytes(L) : 0; }
+
+int tg_checkpoint_save(tg_lattice* L, void* buf, size_t size) {
+  if (!L || !buf) return fail(TG_E_ARG, "null argument");
+  if (size < ckpt_bytes(L)) return fail(TG_E_ARG, "checkpoint buffer too small");
+  CkptHeader h{};
+  memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.nt = L->P.nt;
+  h.nx = L->P.nx;
+  h.bc_t = L->P.bc_t;
+  h.bc_x = L->P.bc_x;
+  h.mt_avail = L->mt.avail;
+  h.mt_seeded = L->mt_seeded ? 1 : 0;
+  h.m = L->P.m;
+  h.g = L->P.g;
+  h.mu = L->P.mu;
+  unsigned long long tr = 0;
+  TG_CK(cudaMemcpyAsync(&tr, &L->ts->traj, sizeof tr, cudaMemcpyDeviceToHost, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  h.traj = tr;
+  unsigned char* q = static_cast<unsigned char*>(buf);
+  memcpy(q, &h, sizeof h);
+  q += sizeof h;
+  memcpy(q, L->mt.w, sizeof L->mt.w);
+  q += sizeof L->mt.w;
+  memcpy(q, L->mt.out, sizeof L->mt.out);
+  q += sizeof L->mt.out;
+  TG_TRY(download(L, reinterpret_cast<double*>(q), L->A, 2 * (size_t)L->V));
+  return TG_OK;
+}
+
+int tg_checkpoint_load(tg_lattice* L, const void* buf, size_t size) {
+  if (!L || !buf) return fail(TG_E_ARG, "null argument");
+  CkptHeader h;
+  if (size < sizeof h) return fail(TG_E_ARG, "not a checkpoint");
+  memcpy(&h, buf, sizeof h);
+  if (memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1) return fail(TG_E_ARG, "not a checkpoint");
+  if (h.nt != L->P.nt || h.nx != L->P.nx || h.bc_t != L->P.bc_t || h.bc_x != L->P.bc_x)
+    return fail(TG_E_ARG, "checkpoint of another lattice (size or boundary conditions)");
+  if (size < ckpt_bytes(L)) return fail(TG_E_ARG, "checkpoint truncated");
+  if (h.mt_avail < 0 || h.mt_avail > 624) return fail(TG_E_ARG, "corrupt checkpoint (MT state)");
+  const unsigned char* q = static_cast<const unsigned char*>(buf) + sizeof h;
+  TG_TRY(tg_set_couplings(L, h.m, h.g, h.mu));
+  memcpy(L->mt.w, q, sizeof L->mt.w);
+  q += sizeof L->mt.w;
+  memcpy(L->mt.out, q, sizeof L->mt.out);
+  q += sizeof L->mt.out;
+  L->mt.avail = h.mt_avail;
+  L->mt_seeded = h.mt_seeded != 0;
+  TG_TRY(tg_set_gauge(L, reinterpret_cast<const double*>(q)));
+  const unsigned long long tr = h.traj;
+  TG_CK(cudaMemcpyAsync(&L->ts->traj, &tr, sizeof tr, cudaMemcpyHostToDevice, L->stream));
+  TG_CK(cudaStreamSynchronize(L->stream));
+  return TG_OK;
+}
+
 int tg_mt_uniforms(tg_lattice* L, double* out, long n) {
   if (!L || (!out && n > 0) || n < 0) return fail(TG_E_ARG, "bad argument");
   for (long i = 0; i < n; i++) out[i] = L->mt.next();

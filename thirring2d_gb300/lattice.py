@@ -86,6 +86,26 @@ class Lattice:
         N.check(self.lib.tg_get_gauge(self.h, _p(A)))
         return A
 
+    # -- checkpoint and resume ------------------------------------------------
+    def checkpoint(self) -> bytes:
+        """The lattice's state (couplings, MT stream, Philox counter, A) as bytes."""
+        n = self.lib.tg_checkpoint_size(self.h)
+        buf = (C.c_ubyte * n)()
+        N.check(self.lib.tg_checkpoint_save(self.h, buf, n))
+        return bytes(buf)
+
+    def restore(self, data: bytes):
+        buf = (C.c_ubyte * len(data)).from_buffer_copy(data)
+        N.check(self.lib.tg_checkpoint_load(self.h, buf, len(data)))
+
+    def save(self, path: str):
+        with open(path, "wb") as f:
+            f.write(self.checkpoint())
+
+    def load(self, path: str):
+        with open(path, "rb") as f:
+            self.restore(f.read())
+
     def synchronize(self):
         N.check(self.lib.tg_synchronize(self.h))
 
