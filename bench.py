@@ -428,70 +428,84 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
     """The batched-chain workload (512 chains, sides in {16..128}, m ~ U[0.05, 0.5],
     g ~ U[0.2, 1.2], 10 leapfrog steps, CG 1e-10): mixed-precision batch in one
     launch per trajectory vs the same chains one at a time on the plain FP64
-    single-lattice path (a sample of `sample` chains, scaled)."""
+    single-lattice path (a sample of `sample` chains, scaled).  The same
+    comparison is repeated at CG 1e-12, where the mixed batch matches the FP64
+    batch's dH to 1e-9 on every chain whose MD is stable."""
     from thirring2d_gb300.profile_case import mixed_size_chains
     chains, fields = mixed_size_chains(nchains)
-    cgm = tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=tg.native.PREC_MIXED, ru_interval=50)
-    cg64 = tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=tg.native.PREC_FP64)
+    steps = max(1, args.steps)
 
-    def make(cg):
+    def cg(prec, tol):
+        return tg.cg_params(rel_tol=tol, abs_tol2=0.0, precision=prec, ru_interval=50)
+
+    def make(c, block=0):
         B = tg.Batch(chains)
         for i, A in enumerate(fields):
             B.set_gauge(i, A)
-        return B, tg.batch_params(nsteps=10, cg=cg)
+        return B, tg.batch_params(nsteps=10, cg=c, block=block)
 
-    Bm, bpm = make(cgm)
-    cfg, _ = Bm.autotune(bpm)
-    B64, bp64 = make(cg64)
-    first_m, first_64 = Bm.trajectory(bpm), B64.trajectory(bp64)   # same fields, same Philox stream
-    dh_err = max(abs(a.dH - b.dH) / max(1.0, abs(b.dH)) for a, b in zip(first_m, first_64))
-    acc_mismatch = sum(a.accepted != b.accepted for a, b in zip(first_m, first_64))
-    # chains whose MD is stable at this step size (|dH| < 5): the absolute dH error there
-    stable = [(a, b) for a, b in zip(first_m, first_64) if abs(b.dH) < 5.0]
-    dh_err_stable = max((abs(a.dH - b.dH) for a, b in stable), default=0.0)
-    iters64 = [r.cg_iterations for r in first_64]
-    B64.close()
-    steps = max(1, args.steps)
-    ms = 0.0
-    res = []
-    for _ in range(steps):
-        r = Bm.trajectory(bpm)
-        ms += r[0].cg_ms
-        res.append(r)
-    batched_rate = nchains * steps / (ms / 1e3)
-    # one at a time on the FP64 single-lattice path: one warm-up trajectory per
-    # chain (graph capture), then one timed with CUDA events on its stream
-    seq_ms = 0.0
-    for c, A in list(zip(chains, fields))[:sample]:
-        L = tg.Lattice(c["nt"], c["nx"], c["m"], c["g"], c["mu"], c["bc_t"], c["bc_x"])
-        L.set_gauge(A)
-        hp = tg.hmc_params(nsteps=10, rng=tg.native.RNG_PHILOX, seed=c["seed"], cg=cg64)
-        L.update_gauge(hp)
-        st = torch.cuda.ExternalStream(L.lib.tg_stream(L.h), device=dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        L.update_gauge(hp)
-        e1.record(st)
-        torch.cuda.synchronize()
-        seq_ms += e0.elapsed_time(e1)
-        L.close()
-    seq_rate = sample / (seq_ms / 1e3)
-    Bm.close()
-    cpu = cpu_batch_sample(chains, iters64)
-    return {"value": batched_rate, "unit": "chain-trajectories/s", "chains": nchains,
-            "sites": int(sum(c["nt"] * c["nx"] for c in chains)), "precision": "mixed (FP32 CG + FP64 reliable updates)",
-            "kernel_instance": cfg, "ms_per_batch_trajectory": ms / steps,
-            "sequential_fp64": {"value": seq_rate, "unit": "chain-trajectories/s",
+    def sequential(c):
+        # one at a time on the FP64 single-lattice path: one warm-up trajectory
+        # per chain (graph capture), then one timed with CUDA events on its stream
+        seq_ms = 0.0
+        for ch, A in list(zip(chains, fields))[:sample]:
+            L = tg.Lattice(ch["nt"], ch["nx"], ch["m"], ch["g"], ch["mu"], ch["bc_t"], ch["bc_x"])
+            L.set_gauge(A)
+            hp = tg.hmc_params(nsteps=10, rng=tg.native.RNG_PHILOX, seed=ch["seed"], cg=c)
+            L.update_gauge(hp)
+            st = torch.cuda.ExternalStream(L.lib.tg_stream(L.h), device=dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            L.update_gauge(hp)
+            e1.record(st)
+            torch.cuda.synchronize()
+            seq_ms += e0.elapsed_time(e1)
+            L.close()
+        return sample / (seq_ms / 1e3)
+
+    def compare(tol, block):
+        """First trajectory of the mixed and the FP64 batch from the same fields
+        and Philox stream, then `steps` timed mixed trajectories."""
+        Bm, bpm = make(cg(tg.native.PREC_MIXED, tol), block)
+        if block == 0:
+            block, _ = Bm.autotune(bpm)
+            bpm = tg.batch_params(nsteps=10, cg=cg(tg.native.PREC_MIXED, tol), block=block)
+        B64, bp64 = make(cg(tg.native.PREC_FP64, tol), block)
+        first_m, first_64 = Bm.trajectory(bpm), B64.trajectory(bp64)
+        B64.close()
+        # chains whose MD is stable at this step size (|dH| < 5): the absolute dH error there
+        stable = [(a, b) for a, b in zip(first_m, first_64) if abs(b.dH) < 5.0]
+        ms, res = 0.0, []
+        for _ in range(steps):
+            r = Bm.trajectory(bpm)
+            ms += r[0].cg_ms
+            res.append(r)
+        Bm.close()
+        rate = nchains * steps / (ms / 1e3)
+        seq = sequential(cg(tg.native.PREC_FP64, tol))
+        return block, [r.cg_iterations for r in first_64], {
+            "value": rate, "unit": "chain-trajectories/s", "cg_rel_tol": tol, "ms_per_batch_trajectory": ms / steps,
+            "sequential_fp64": {"value": seq, "unit": "chain-trajectories/s",
                                 "sample": f"{sample} of the {nchains} chains, one at a time, second trajectory each"},
-            "speedup_vs_sequential_fp64": batched_rate / seq_rate,
-            "cpu_reference": cpu,
+            "speedup_vs_sequential_fp64": rate / seq,
             "dH_vs_fp64_batch": {
-                "stable_chains": len(stable), "max_abs_err_stable_chains": dh_err_stable,
-                "max_rel_err_all_chains": dh_err, "accept_mismatch": acc_mismatch,
-                "note": "chains with |dH| >= 5 have unstable MD at this step size, where dH differs "
-                        "chaotically between precisions; the decisions still agree"},
+                "stable_chains": len(stable),
+                "max_abs_err_stable_chains": max((abs(a.dH - b.dH) for a, b in stable), default=0.0),
+                "max_rel_err_all_chains": max(abs(a.dH - b.dH) / max(1.0, abs(b.dH))
+                                              for a, b in zip(first_m, first_64)),
+                "accept_mismatch": sum(a.accepted != b.accepted for a, b in zip(first_m, first_64))},
             "acceptance": float(np.mean([r.accepted for r in res[-1]])),
             "cg_iterations_per_chain_traj": float(np.mean([r.cg_iterations for r in res[-1]]))}
+
+    cfg, iters64, main = compare(1e-10, 0)
+    _, _, matched = compare(1e-12, cfg)
+    main["dH_vs_fp64_batch"]["note"] = ("chains with |dH| >= 5 have unstable MD at this step size, where dH differs "
+                                        "chaotically between precisions; the decisions still agree")
+    out = {"chains": nchains, "sites": int(sum(c["nt"] * c["nx"] for c in chains)),
+           "precision": "mixed (FP32 CG + FP64 reliable updates)", "kernel_instance": cfg} | main
+    out["matched_accuracy"] = matched
+    out["cpu_reference"] = cpu_batch_sample(chains, iters64)
+    return out
 
 
 def main():

@@ -140,3 +140,26 @@ def test_cluster_instances_match_block_instance(tg, instance):
     assert tight >= 8
     for k in np.where(same)[0]:
         assert np.abs(runs[51201, "A"][k] - runs[instance, "A"][k]).max() < 1e-8
+
+
+def test_batch_mixed_dH_within_1e9_at_tight_tolerance(tg):
+    """The matched-accuracy claim: with CG at 1e-12, the mixed-precision batch
+    reproduces the FP64 batch's dH to 1e-9 on every chain whose MD is stable
+    (|dH| < 5 at this step size), and makes the same accept/reject decisions on
+    all chains."""
+    from thirring2d_gb300.profile_case import mixed_size_chains
+    chains, fields = mixed_size_chains(128)
+    out = []
+    for precision in (0, 1):
+        B = make_batch(tg, chains, fields)
+        cg = tg.cg_params(rel_tol=1e-12, abs_tol2=0.0, precision=precision, ru_interval=50)
+        out.append(B.trajectory(tg.batch_params(nsteps=10, cg=cg)))
+        B.close()
+    stable = 0
+    for k, (a, b) in enumerate(zip(*out)):
+        assert a.status == 0 and b.status == 0
+        assert a.accepted == b.accepted, (k, a.dH, b.dH)
+        if abs(a.dH) < 5:
+            stable += 1
+            assert abs(a.dH - b.dH) <= 1e-9, (k, a.dH, b.dH)
+    assert stable >= 5
