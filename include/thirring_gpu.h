@@ -315,7 +315,10 @@ typedef struct {
                                per block (one block per chain); or an instance id as
                                tg_batch_autotune reports it (block * 100 + 10 * blocks
                                per chain, when a thread-block cluster of 2 or 4 blocks
-                               runs each chain, + minimum resident blocks per SM)   */
+                               runs each chain, + minimum resident blocks per SM,
+                               + 100000 * S / 1024 when the cluster's blocks split up
+                               to run the chains of at most S = 4096 or 9216 sites
+                               one per block)                                      */
   tg_cg_params cg;          /* per-chain solver                                */
 } tg_batch_params;
 
@@ -331,10 +334,11 @@ int tg_batch_get_gauge(tg_batch* B, int chain, double* A);
 int tg_batch_trajectory(tg_batch* B, const tg_batch_params* p, tg_traj_result* results);
 /* Times one trajectory with every compiled instance of the batch kernel
  * (threads per block x minimum resident blocks per SM, which trades registers
- * against occupancy, and one block or a cluster of 2 or 4 blocks per chain),
+ * against occupancy, one block or a cluster of 2 or 4 blocks per chain, and
+ * whether a cluster's blocks take the smallest chains one each),
  * with the chains' state saved and restored around every trial, and makes the
  * fastest the default (p->block = 0).  *best_block = the winner's instance id
- * (100 * threads + 10 * blocks per chain if clustered + blocks per SM);
+ * (as for tg_batch_params.block);
  * *best_ms = its device time. */
 int tg_batch_autotune(tg_batch* B, const tg_batch_params* p, int* best_block, double* best_ms);
 

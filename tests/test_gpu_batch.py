@@ -101,7 +101,7 @@ def test_batch_mixed_sizes_many_chains(tg):
         prev = res
 
 
-@pytest.mark.parametrize("instance", [51221, 51241, 25641])
+@pytest.mark.parametrize("instance", [51221, 51241, 25641, 451221, 951241])
 def test_cluster_instances_match_block_instance(tg, instance):
     """Chains split over thread-block clusters (2 or 4 blocks, distributed
     shared memory sums) against one block per chain: the same trajectories to

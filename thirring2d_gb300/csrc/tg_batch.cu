@@ -19,9 +19,20 @@ __global__ void __launch_bounds__(BS, MINB) k_batch_trajectory(const BatchChain*
 // minimum resident blocks per SM).  More blocks per SM cap the registers (64 at
 // 2048 resident threads, with spills in the column march); fewer leave room
 // for the march's registers (up to 255 at 256 threads and one block).
-// The cluster instances split each chain over 2 or 4 SMs.
-const BatchCfg kBatchCfgs[kBatchNumCfgs] = {{128, 8, 1}, {256, 4, 1}, {256, 2, 1}, {256, 1, 1}, {384, 1, 1},
-                                            {512, 1, 1}, {512, 1, 2}, {512, 1, 4}, {256, 1, 4}};
+// The cluster instances split each chain over 2 or 4 SMs; their variants with
+// solo_sites hand the chains of up to 64^2 or 96^2 sites (the end of the
+// largest-first queue) to single blocks, which no longer wait on cluster
+// barriers.
+const BatchCfg kBatchCfgs[kBatchNumCfgs] = {
+    {128, 8, 1, 0},    {256, 4, 1, 0},    {256, 2, 1, 0},    {256, 1, 1, 0},    {384, 1, 1, 0},
+    {512, 1, 1, 0},    {512, 1, 2, 0},    {512, 1, 4, 0},    {256, 1, 4, 0},    {512, 1, 2, 4096},
+    {512, 1, 2, 9216}, {512, 1, 4, 4096}, {512, 1, 4, 9216}, {256, 1, 4, 4096}, {256, 1, 4, 9216}};
+
+// the cluster kernel of instance cfg (see batch_cluster_max)
+static int cluster_kernel_of(int cfg) {
+  const BatchCfg& c = kBatchCfgs[cfg];
+  return c.cluster == 2 ? 0 : (c.block == 512 ? 1 : 2);
+}
 
 template <int BS, int MINB> const void* batch_kernel() { return (const void*)k_batch_trajectory<BS, MINB>; }
 
@@ -49,7 +60,7 @@ static void launch_blocks(cudaStream_t s, int cfg, int grid, const BatchChain* c
 }
 
 int batch_teams(int cfg, int sms) {
-  if (kBatchCfgs[cfg].cluster > 1) return batch_cluster_max(cfg - 6);
+  if (kBatchCfgs[cfg].cluster > 1) return batch_cluster_max(cluster_kernel_of(cfg));
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_kernel_of(cfg), kBatchCfgs[cfg].block, 0) !=
       cudaSuccess)
@@ -60,7 +71,8 @@ int batch_teams(int cfg, int sms) {
 void batch_trajectory(cudaStream_t s, int cfg, int sms, const BatchChain* chains, const int* order, int n,
                       const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue) {
   const int teams = std::min(n, std::max(1, batch_teams(cfg, sms)));
-  if (kBatchCfgs[cfg].cluster > 1) batch_cluster_launch(s, cfg - 6, teams, chains, order, n, F, P, results, queue);
+  if (kBatchCfgs[cfg].cluster > 1)
+    batch_cluster_launch(s, cluster_kernel_of(cfg), teams, chains, order, n, F, P, results, queue);
   else launch_blocks(s, cfg, teams, chains, order, n, F, P, results, queue);
 }
 

@@ -32,6 +32,9 @@ struct BatchTraj {
   double tau;
   int stochastic_term;
   BatchCg cg;
+  // cluster instances: from this queue position on, every block of a cluster
+  // runs chains of its own (n: never)
+  int solo_from;
 };
 
 // Per-chain outcome of a trajectory; `traj` is the chain's Philox trajectory
@@ -43,11 +46,13 @@ struct ChainResult {
 };
 
 // kernel instances of the batched trajectory: threads per block, min blocks per
-// SM, and blocks per chain (1: one block per chain; > 1: a thread-block cluster)
+// SM, blocks per chain (1: one block per chain; > 1: a thread-block cluster),
+// and for clusters the chain size (sites) at or below which the cluster's
+// blocks split up and run one chain each (0: never)
 struct BatchCfg {
-  int block, minb, cluster;
+  int block, minb, cluster, solo_sites;
 };
-constexpr int kBatchNumCfgs = 9;
+constexpr int kBatchNumCfgs = 15;
 extern const BatchCfg kBatchCfgs[kBatchNumCfgs];
 
 // Launches instance cfg over n chains with as many teams as can be resident.
@@ -55,8 +60,11 @@ void batch_trajectory(cudaStream_t s, int cfg, int sms, const BatchChain* chains
                       const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue);
 // teams (blocks or clusters) of instance cfg that can be resident at once (0: cannot launch)
 int batch_teams(int cfg, int sms);
-// the tuned instance as reported to callers: block * 100 + 10 * cluster (if > 1) + min blocks per SM
-inline int batch_cfg_id(const BatchCfg& c) { return c.block * 100 + (c.cluster > 1 ? 10 * c.cluster : 0) + c.minb; }
+// the tuned instance as reported to callers: block * 100 + 10 * cluster (if > 1)
+// + min blocks per SM, + 100000 * (solo_sites / 1024)
+inline int batch_cfg_id(const BatchCfg& c) {
+  return c.block * 100 + (c.cluster > 1 ? 10 * c.cluster : 0) + c.minb + 100000 * (c.solo_sites / 1024);
+}
 
 // tg_batch_cluster.cu: instance `which` (0: 512 x 2 blocks, 1: 512 x 4, 2: 256 x 4)
 int batch_cluster_max(int which);

@@ -33,25 +33,63 @@ __device__ __forceinline__ double warp_allsum(double v) {
   return v;
 }
 
-// Deterministic block sum returned to every thread (fixed butterfly order).
-__device__ __forceinline__ double bsum(double v) {
-  __shared__ double sh[32];
+// Shared scratch of the team sums: the warps' partials, the block's total (read
+// by the other blocks of a cluster) and the result of the step that follows a
+// sum.
+struct TeamScratch {
+  double part[32];
+  double total[2];  // a cluster's block totals alternate between two slots
+  double out[4];
+  int phase;        // the slot of the next sum (thread 0 only)
+};
+__device__ __forceinline__ TeamScratch& team_scratch() {
+  __shared__ TeamScratch sc;
+  return sc;
+}
+
+__device__ __forceinline__ float warp_allsum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// The block's total of the threads' partials (fixed butterfly order), in warp
+// 0.  FP32 partials are added in FP32 within a warp (their own rounding is
+// FP32's already) and in FP64 from the warps' totals on.
+template <typename P> __device__ __forceinline__ double block_total_warp0(P v, TeamScratch& sc) {
   v = warp_allsum(v);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __syncthreads();  // the previous call's readers are done with sh
-  if (lane == 0) sh[w] = v;
+  if (lane == 0) sc.part[w] = (double)v;
   __syncthreads();  // also publishes every global write made before the call
-  return warp_allsum(lane < nw ? sh[lane] : 0.0);
+  return w == 0 ? warp_allsum(lane < nw ? sc.part[lane] : 0.0) : 0.0;
 }
 
 // A team runs one chain.  It gives the chain-wide loop over sites, barrier and
 // sum; every thread of the team sees the same sums (fixed order), so all make
 // the same decisions and the team's control flow stays uniform.
+//
+// sum_then(v, f): the team's total of the threads' partials v, handed to f,
+// which runs once per block (thread 0); every thread gets f's result (a small
+// trivially copyable struct).  Scalars derived from a sum -- CG step lengths,
+// the stopping tests -- are computed there once instead of in every thread:
+// the FP64 pipe retires two operations per SM per clock, and one double
+// division is about ten of them.
 struct BlockTeam {  // one thread block
   __device__ static int rank() { return 0; }
   __device__ static int nblocks() { return 1; }
   __device__ static void sync() { __syncthreads(); }
-  __device__ static double sum(double v) { return bsum(v); }
+  template <typename P, class F> __device__ static auto sum_then(P v, F f) -> decltype(f(0.0)) {
+    using S = decltype(f(0.0));
+    static_assert(sizeof(S) <= sizeof(TeamScratch::out), "sum_then result too large");
+    TeamScratch& sc = team_scratch();
+    const double t = block_total_warp0(v, sc);
+    if (threadIdx.x == 0) *reinterpret_cast<S*>(sc.out) = f(t);
+    __syncthreads();
+    return *reinterpret_cast<const S*>(sc.out);
+  }
+  __device__ static double sum(double v) { return sum_then(v, [](double t) { return t; }); }
+  __device__ static void init() {}
+  static constexpr bool kCluster = false;
   // the queue ticket thread 0 of rank 0 wrote to `next`
   __device__ static int broadcast(const int* next) {
     __syncthreads();
@@ -61,22 +99,42 @@ struct BlockTeam {  // one thread block
 
 // CL thread blocks of one cluster, on CL SMs.  The cluster barrier orders
 // the blocks' global and shared memory accesses; sums combine the blocks'
-// partials through distributed shared memory.
+// totals through distributed shared memory, in the same order in every block,
+// so the blocks stay in lockstep.
 template <int CL> struct ClusterTeam {
   __device__ static int rank() { return (int)cooperative_groups::this_cluster().block_rank(); }
   __device__ static int nblocks() { return CL; }
   __device__ static void sync() { cooperative_groups::this_cluster().sync(); }
-  __device__ static double sum(double v) {
-    __shared__ double part;
-    const double b = bsum(v);
-    if (threadIdx.x == 0) part = b;
+  template <typename P, class F> __device__ static auto sum_then(P v, F f) -> decltype(f(0.0)) {
+    using S = decltype(f(0.0));
+    static_assert(sizeof(S) <= sizeof(TeamScratch::out), "sum_then result too large");
+    TeamScratch& sc = team_scratch();
+    const double b = block_total_warp0(v, sc);
+    int ph = 0;
+    if (threadIdx.x == 0) {
+      ph = sc.phase;
+      sc.total[ph] = b;
+    }
     cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
-    cl.sync();  // every block's partial is written
-    double s = 0;
-    for (int r = 0; r < CL; r++) s += *cl.map_shared_rank(&part, r);  // the same order in every thread
-    cl.sync();  // every thread has read before the next call overwrites part
-    return s;
+    cl.sync();  // every block's total is written, with every write made before the call
+    if (threadIdx.x == 0) {
+      double s = 0;
+      for (int r = 0; r < CL; r++) s += cl.map_shared_rank(sc.total, r)[ph];
+      *reinterpret_cast<S*>(sc.out) = f(s);
+      sc.phase = ph ^ 1;
+    }
+    // A block barrier publishes out.  The slot just read is written again two
+    // sums later, after the next sum's cluster barrier, which no block passes
+    // before every block has finished reading it.
+    __syncthreads();
+    return *reinterpret_cast<const S*>(sc.out);
   }
+  static constexpr bool kCluster = true;
+  // every block of the cluster starts with the same slot
+  __device__ static void init() {
+    if (threadIdx.x == 0) team_scratch().phase = 0;
+  }
+  __device__ static double sum(double v) { return sum_then(v, [](double t) { return t; }); }
   __device__ static int broadcast(const int* next) {
     cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
     cl.sync();
@@ -102,6 +160,19 @@ struct ChainCtx {
 
 struct CgOut {
   int iter, status, n_ru;
+};
+
+// What the CG loops need after the |r|^2 sum: the sum, beta, and the verdict
+// of the stopping tests (FP64: a status, or -1 to go on; mixed: whether a
+// reliable update is due, which runs the tests on the true residual).
+struct CgTail64 {
+  double rn, beta;
+  int status;
+};
+struct CgTailMx {
+  double rn;
+  float fb;
+  int need;
 };
 
 // ---------------------------------------------------------------------------
@@ -149,7 +220,7 @@ __device__ CgOut block_cg64(const ChainCtx& c, const BatchCg& P, const double2* 
       v = fma(o.y, o.y, v);
     };
     stencil_team<T, double, 0, MU0>(c.g, km, ld, c.Wt, c.Wx, epi);
-    const double alpha = rr / T::sum(v);
+    const double alpha = T::sum_then(v, [&](double pAp) { return rr / pAp; });
     v = 0;
     auto ld2 = [&](int i) { return c.Mp64[i]; };
     auto epi2 = [&](int s, double2 ap, double2) {
@@ -164,15 +235,22 @@ __device__ CgOut block_cg64(const ChainCtx& c, const BatchCg& P, const double2* 
       v = fma(rv.y, rv.y, v);
     };
     stencil_team<T, double, 1, MU0>(c.g, kd, ld2, c.Wt, c.Wx, epi2);
-    const double rn = T::sum(v);
+    const CgTail64 e = T::sum_then(v, [&](double rn) {
+      CgTail64 o{rn, rn / rr, -1};
+      if (isnan(rn)) o.status = TG_E_NAN;
+      else if (rn < stop) o.status = TG_OK;
+      else if (rn / rr0 > 1e10) o.status = TG_E_DIVERGED;
+      else if (out.iter + 1 >= P.maxiter) o.status = TG_E_NOCONV;
+      return o;
+    });
     half ^= 1;
     out.iter++;
-    beta = rn / rr;
-    rr = rn;
-    if (isnan(rn)) { out.status = TG_E_NAN; break; }
-    if (rn < stop) { out.status = TG_OK; break; }
-    if (rn / rr0 > 1e10) { out.status = TG_E_DIVERGED; break; }
-    if (out.iter >= P.maxiter) { out.status = TG_E_NOCONV; break; }
+    beta = e.beta;
+    rr = e.rn;
+    if (e.status >= 0) {
+      out.status = e.status;
+      break;
+    }
   }
   T::sync();
   return out;
@@ -201,10 +279,10 @@ __device__ CgOut block_cg_mixed(const ChainCtx& c, const BatchCg& P, const doubl
     out.status = isnan(rr0) ? TG_E_NAN : TG_OK;
     return out;
   }
-  double rr = rr0, rr_true = rr0, beta = 0;
+  double rr = rr0, rr_true = rr0;
+  float fb = 0.f;
   int since = 0, half = 0;
   while (true) {
-    const float fb = (float)beta;
     const float2* p_old = half ? c.ps2 : c.ps;
     float2* p_new = half ? c.ps : c.ps2;
     float v = 0;
@@ -219,8 +297,7 @@ __device__ CgOut block_cg_mixed(const ChainCtx& c, const BatchCg& P, const doubl
       v = fmaf(o.y, o.y, v);
     };
     stencil_team<T, float, 0, MU0>(c.g, km32, ld, c.Wt32, c.Wx32, epi);
-    const double alpha = rr / T::sum((double)v);
-    const float fa = (float)alpha;
+    const float fa = T::sum_then(v, [&](double pAp) { return (float)(rr / pAp); });
     v = 0;
     auto ld2 = [&](int i) { return c.Mps[i]; };
     auto epi2 = [&](int s, float2 ap, float2) {
@@ -235,15 +312,18 @@ __device__ CgOut block_cg_mixed(const ChainCtx& c, const BatchCg& P, const doubl
       v = fmaf(rv.y, rv.y, v);
     };
     stencil_team<T, float, 1, MU0>(c.g, kd32, ld2, c.Wt32, c.Wx32, epi2);
-    const double rn = T::sum((double)v);
+    const CgTailMx e = T::sum_then(v, [&](double rn) {
+      CgTailMx o{rn, (float)(rn / rr), 0};
+      o.need = since + 1 >= P.ru_interval || rn < stop || rn < kRuDrop * rr_true || out.iter + 1 >= P.maxiter ||
+               rn / rr0 > 1e10 || isnan(rn);
+      return o;
+    });
     half ^= 1;
     out.iter++;
     since++;
-    beta = rn / rr;
-    rr = rn;
-    const bool need = since >= P.ru_interval || rn < stop || rn < kRuDrop * rr_true || out.iter >= P.maxiter ||
-                      rn / rr0 > 1e10 || isnan(rn);
-    if (!need) continue;
+    fb = e.fb;
+    rr = e.rn;
+    if (!e.need) continue;
     // reliable update: x += xs, r = b - M^dag M x in FP64
     TG_BSITES(s, V) {
       float2 d = c.xs[s];
@@ -266,7 +346,7 @@ __device__ CgOut block_cg_mixed(const ChainCtx& c, const BatchCg& P, const doubl
       a2 = fma(rv.y, rv.y, a2);
     }
     const double rt = T::sum(a2);
-    if (rt > kRuRestart * rr) beta = 0;  // recursive residual far too optimistic: restart p from r
+    if (rt > kRuRestart * rr) fb = 0.f;  // recursive residual far too optimistic: restart p from r
     rr = rt;
     rr_true = rt;
     since = 0;
@@ -345,10 +425,16 @@ __device__ void chain_trajectory(const ChainCtx& c, const BatchTraj& P, ChainRes
     n_ru += o.n_ru;
     status = max(status, o.status);
     if (i == P.nsteps) break;  // the last solve gives S_pf at the end
-    TG_BSITES(s, V) c.Mx[s] = dslash_at<double, 0, MU0>(g, km, c.x, c.Wt, c.Wx, s);
-    T::sync();
+    // M x: a mixed solve ends on a reliable update, which left M x of the final x
+    // in tmp (the same function of the same operands); otherwise apply M.
+    const double2* Mx = c.tmp;
+    if (P.cg.precision != TG_PREC_MIXED || o.n_ru == 0) {
+      TG_BSITES(s, V) c.Mx[s] = dslash_at<double, 0, MU0>(g, km, c.x, c.Wt, c.Wx, s);
+      T::sync();
+      Mx = c.Mx;
+    }
     TG_BSITES(s, V) {
-      ForcePieces f = force_site(g, c.bc_t, c.bc_x, c.ep, c.em, c.An, c.Wt, c.Wx, c.x, c.Mx,
+      ForcePieces f = force_site(g, c.bc_t, c.bc_x, c.ep, c.em, c.An, c.Wt, c.Wx, c.x, Mx,
                                  noise_on ? c.noise : nullptr, s);
       double2 p = c.mom[s];
       p.x -= gfac * f.g.x;
@@ -424,15 +510,38 @@ __device__ __forceinline__ void batch_trajectory_body(const BatchChain* __restri
   // block of a team fills its own copy.
   __shared__ int next;
   __shared__ ChainCtx c;
+  T::init();  // published by the first broadcast's barriers
+  int q;
   while (true) {
     if (T::rank() == 0 && threadIdx.x == 0) next = (int)atomicAdd(queue, 1u);
-    const int q = T::broadcast(&next);
-    if (q >= n) break;
+    q = T::broadcast(&next);
+    if (q >= n || (T::kCluster && q >= P.solo_from)) break;
     const int ci = order[q];
     if (threadIdx.x == 0) fill_ctx(c, chains[ci], F);
     __syncthreads();
     if (c.mu == 0.0) chain_trajectory<true, T>(c, P, &results[ci]);
     else chain_trajectory<false, T>(c, P, &results[ci]);
+  }
+  if constexpr (T::kCluster) {
+    // The rest of the queue holds small chains: rank 0 runs chain q and every
+    // block then takes chains of its own, with block barriers only.  No block
+    // touches another's shared memory from here on (the broadcast's closing
+    // cluster barrier has ordered every earlier access).
+    int mine = (q < n && T::rank() == 0) ? q : -1;
+    while (true) {
+      if (mine < 0) {
+        if (threadIdx.x == 0) next = (int)atomicAdd(queue, 1u);
+        __syncthreads();
+        mine = next;
+        if (mine >= n) break;
+      }
+      const int ci = order[mine];
+      if (threadIdx.x == 0) fill_ctx(c, chains[ci], F);
+      __syncthreads();
+      if (c.mu == 0.0) chain_trajectory<true, BlockTeam>(c, P, &results[ci]);
+      else chain_trajectory<false, BlockTeam>(c, P, &results[ci]);
+      mine = -1;
+    }
   }
 }
 

@@ -1420,6 +1420,7 @@ struct tg_batch {
   long long total = 0;
   std::vector<tg_chain_params> P;
   std::vector<long long> off;
+  std::vector<int> order;  // the work queue: chains by estimated cost, largest first
   cudaStream_t stream = nullptr;
   BatchChain* d_chains = nullptr;
   int* d_order = nullptr;
@@ -1455,6 +1456,14 @@ int batch_launch(tg_batch* B, const tg_batch_params& p, int cfg, cudaStream_t s)
   t.tau = p.tau;
   t.stochastic_term = p.stochastic_term;
   t.cg = BatchCg{p.cg.rel_tol, p.cg.abs_tol2, p.cg.maxiter, p.cg.precision, p.cg.ru_interval};
+  // cluster instances with solo_sites: single blocks from the first queued chain that small
+  t.solo_from = B->n;
+  if (kBatchCfgs[cfg].cluster > 1 && kBatchCfgs[cfg].solo_sites > 0)
+    for (int q = 0; q < B->n; q++)
+      if ((long long)B->P[B->order[q]].nt * B->P[B->order[q]].nx <= kBatchCfgs[cfg].solo_sites) {
+        t.solo_from = q;
+        break;
+      }
   TG_CK(cudaMemsetAsync(B->d_queue, 0, sizeof(unsigned), s));
   batch_trajectory(s, cfg, B->sms, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
   TG_CK(cudaGetLastError());
@@ -1570,6 +1579,7 @@ int tg_batch_create(const tg_chain_params* chains, int nchains, int device, tg_b
     return bail(rc);
   if (cudaMallocHost((void**)&B->h_res, sizeof(ChainResult) * nchains) != cudaSuccess)
     return bail(fail(TG_E_ALLOC, "pinned allocation failed"));
+  B->order = order;
   if (cudaMemcpyAsync(B->d_chains, hc.data(), sizeof(BatchChain) * nchains, cudaMemcpyHostToDevice, B->stream) !=
           cudaSuccess ||
       cudaMemcpyAsync(B->d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, B->stream) !=

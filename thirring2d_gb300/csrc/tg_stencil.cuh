@@ -80,8 +80,30 @@ __device__ __forceinline__ void march_segment(const Geo& g, const OpK<R>& k, Ld&
   for (; t + kMarchT <= tb; t += kMarchT) {
     C2<R> ep, ew;
     edge_operands<R>(g, ld, Wx, t, xle, xre, lane, ep, ew);
+    if constexpr (sizeof(R) == 4) {
+      // FP32 (memory- or latency-bound): every load of the chunk is issued
+      // before its first result is stored.  The epilogue's stores may alias the
+      // operands as far as the compiler knows, and would otherwise hold each
+      // row's loads behind the previous row's stores, one memory latency per
+      // row.  (The FP64 march is bound by the FP64 pipe and keeps its
+      // registers.)
+      C2<R> pp[kMarchT], wt[kMarchT], wx[kMarchT];
 #pragma unroll
-    for (int i = 0; i < kMarchT; i++) row(t + i, shfl_c2<R>(ep, (lane == 31) ? kMarchT + i : i), shfl_c2<R>(ew, i));
+      for (int i = 0; i < kMarchT; i++) {
+        const int tt = t + i;
+        const int tp = (tt + 1 == g.nt) ? 0 : tt + 1;
+        pp[i] = ld(tp * nx + x);
+        wt[i] = Wt[tt * nx + x];
+        wx[i] = Wx[tt * nx + x];
+      }
+#pragma unroll
+      for (int i = 0; i < kMarchT; i++)
+        march_row<R, DAG, MU0, UNIT>(k, (t + i) * nx + x, lane, pm, pc, wtm, pp[i], wt[i], wx[i],
+                                     shfl_c2<R>(ep, (lane == 31) ? kMarchT + i : i), shfl_c2<R>(ew, i), epi);
+    } else {
+#pragma unroll
+      for (int i = 0; i < kMarchT; i++) row(t + i, shfl_c2<R>(ep, (lane == 31) ? kMarchT + i : i), shfl_c2<R>(ew, i));
+    }
   }
   for (; t < tb; t++) {  // the last rows of the segment: lanes 0 and 31 fetch their own
     const int xe = (lane == 31) ? xre : xle;
