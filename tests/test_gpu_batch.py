@@ -163,3 +163,24 @@ def test_batch_mixed_dH_within_1e9_at_tight_tolerance(tg):
             stable += 1
             assert abs(a.dH - b.dH) <= 1e-9, (k, a.dH, b.dH)
     assert stable >= 5
+
+
+def test_solo_blocks_reproduce_one_block_instance(tg):
+    """A cluster instance with solo blocks runs the chains of at most 64^2 sites
+    one per block, with the one-block code: on a batch of only such chains
+    (every block solo from the first chain on) it reproduces the 512 x 1
+    instance bitwise, whatever block a chain lands on."""
+    chains = [dict(nt=L, nx=L, m=0.2 + 0.05 * k, g=0.6, mu=0.1 * (k % 2), bc_t=-1, bc_x=1, seed=500 + k)
+              for k, L in enumerate([16, 24, 32, 48, 64, 16, 32, 64, 24, 48, 16])]
+    rng = np.random.default_rng(3)
+    fields = [rng.normal(0, 0.2, (c["nt"], c["nx"], 2)) for c in chains]
+    out = {}
+    for inst in (51201, 451241, 451221):
+        B = make_batch(tg, chains, fields)
+        bp = tg.batch_params(nsteps=6, block=inst, cg=tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=1))
+        out[inst] = [[(r.dH, r.accepted, r.cg_iterations) for r in B.trajectory(bp)] for _ in range(2)]
+        out[inst, "A"] = [B.get_gauge(i) for i in range(len(chains))]
+        B.close()
+    for inst in (451241, 451221):
+        assert out[inst] == out[51201]
+        assert all(np.array_equal(a, b) for a, b in zip(out[inst, "A"], out[51201, "A"]))
