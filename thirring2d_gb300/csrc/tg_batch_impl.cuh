@@ -282,36 +282,47 @@ __device__ CgOut block_cg_mixed(const ChainCtx& c, const BatchCg& P, const doubl
   double rr = rr0, rr_true = rr0;
   float fb = 0.f;
   int since = 0, half = 0;
+  // The FP32 iteration's operands, out of the shared-memory context: read
+  // through it, every pointer would be reloaded for each row, since the
+  // compiler cannot tell the rows' global stores from shared memory.
+  const Geo g = c.g;
+  float2* const rs = c.rs;
+  float2* const xs = c.xs;
+  float2* const Mps = c.Mps;
+  float2* const ps_a = c.ps;
+  float2* const ps_b = c.ps2;
+  const float2* const Wt32 = c.Wt32;
+  const float2* const Wx32 = c.Wx32;
   while (true) {
-    const float2* p_old = half ? c.ps2 : c.ps;
-    float2* p_new = half ? c.ps : c.ps2;
+    const float2* p_old = half ? ps_b : ps_a;
+    float2* p_new = half ? ps_a : ps_b;
     float v = 0;
     auto ld = [&](int i) {
-      const float2 rv = c.rs[i], pv = p_old[i];
+      const float2 rv = rs[i], pv = p_old[i];
       return make_float2(fmaf(fb, pv.x, rv.x), fmaf(fb, pv.y, rv.y));
     };
     auto epi = [&](int s, float2 o, float2 pc) {
       p_new[s] = pc;
-      c.Mps[s] = o;
+      Mps[s] = o;
       v = fmaf(o.x, o.x, v);
       v = fmaf(o.y, o.y, v);
     };
-    stencil_team<T, float, 0, MU0>(c.g, km32, ld, c.Wt32, c.Wx32, epi);
+    stencil_team<T, float, 0, MU0>(g, km32, ld, Wt32, Wx32, epi);
     const float fa = T::sum_then(v, [&](double pAp) { return (float)(rr / pAp); });
     v = 0;
-    auto ld2 = [&](int i) { return c.Mps[i]; };
+    auto ld2 = [&](int i) { return Mps[i]; };
     auto epi2 = [&](int s, float2 ap, float2) {
-      float2 xv = c.xs[s], pv = p_new[s], rv = c.rs[s];
+      float2 xv = xs[s], pv = p_new[s], rv = rs[s];
       xv.x = fmaf(fa, pv.x, xv.x);
       xv.y = fmaf(fa, pv.y, xv.y);
       rv.x = fmaf(-fa, ap.x, rv.x);
       rv.y = fmaf(-fa, ap.y, rv.y);
-      c.xs[s] = xv;
-      c.rs[s] = rv;
+      xs[s] = xv;
+      rs[s] = rv;
       v = fmaf(rv.x, rv.x, v);
       v = fmaf(rv.y, rv.y, v);
     };
-    stencil_team<T, float, 1, MU0>(c.g, kd32, ld2, c.Wt32, c.Wx32, epi2);
+    stencil_team<T, float, 1, MU0>(g, kd32, ld2, Wt32, Wx32, epi2);
     const CgTailMx e = T::sum_then(v, [&](double rn) {
       CgTailMx o{rn, (float)(rn / rr), 0};
       o.need = since + 1 >= P.ru_interval || rn < stop || rn < kRuDrop * rr_true || out.iter + 1 >= P.maxiter ||

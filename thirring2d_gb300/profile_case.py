@@ -37,6 +37,7 @@ def main():
     ap.add_argument("--sequential", type=int, default=0, help="chains to also run one at a time (FP64 path)")
     ap.add_argument("--ru-interval", type=int, default=50, help="mixed precision: iterations between reliable updates")
     ap.add_argument("--side", type=int, default=0, help="batched case: give every chain this side")
+    ap.add_argument("--instance", type=int, default=0, help="batched case: this kernel instance, no autotuning")
     ap.add_argument("--scaling-report", action="store_true", help="the 64^2 two-pseudofermion dH-scaling report")
     ap.add_argument("--mixed-report", action="store_true", help="the ill-conditioned (m 0.02) mixed-precision report")
     ap.add_argument("--mixed-tau", type=float, nargs="+", default=[1.0, 0.05],
@@ -93,9 +94,9 @@ def batch_case(a):
     for i, A in enumerate(fields):
         B.set_gauge(i, A)
     prec = N.PREC_MIXED if a.precision == "mixed" else N.PREC_FP64
-    bp = batch_params(nsteps=10, use_graph=bool(a.graph),
+    bp = batch_params(nsteps=10, use_graph=bool(a.graph), block=a.instance,
                       cg=cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=prec, ru_interval=a.ru_interval))
-    block, tune_ms = B.autotune(bp)
+    block, tune_ms = (a.instance, None) if a.instance else B.autotune(bp)
     out = {"chains": a.batch, "sites": B.total_sites(), "precision": a.precision, "block": block,
            "tune_ms": tune_ms, "traj_ms": []}
     for _ in range(a.trajectories):
