@@ -11,9 +11,10 @@ Workload (one "step" = one HMC trajectory of the hot path):
 Output: one JSON line (rank 0).  `value` is device-timed trajectories/s with the
 gauge field resident in HBM; `e2e` the same through the public C ABI with the
 gauge field uploaded from and downloaded to host memory every trajectory.
-`roofline` is the CG iteration (k_cg1 + k_cg2_64, >99% of the device
-time), timed with CUDA events inside the trajectory graph, against the
-algorithmic 208 B/site of one FP64 CG iteration.  Also reported: the operator
+`roofline` is the CG iteration (inside k_pcg64, the persistent FP64 solver:
+one cooperative launch per solve, >99% of the device time), timed with CUDA
+events around the solves inside the trajectory graph, against the algorithmic
+208 B/site of one FP64 CG iteration.  Also reported: the operator
 apply alone (20 M and 20 M^dag applies, 64 B/site) and the same trajectories
 with the mixed-precision solver (FP32 CG + FP64 reliable updates every 50
 iterations) started from the same field and random stream.
@@ -60,9 +61,10 @@ def peaks():
     return 6800.0, "fallback"
 
 
-# DRAM bytes (read + write) of one FP64 CG iteration (k_cg1<double> + k_cg2_64)
-# at 1024^2 from one ncu capture: profiles/cg_iteration_1024_fp64.md.
-CG_ITER_DRAM_BYTES = 182.7e6
+# DRAM bytes (read + write) of one FP64 CG iteration of the persistent solver
+# (k_pcg64, 100 iterations in one launch) at 1024^2 from one ncu capture:
+# profiles/cg_iteration_1024_fp64_persistent.md.
+CG_ITER_DRAM_BYTES = 120.8e6
 # FP64 work of one CG iteration per site, in flops (FMA = 2): two operator
 # applies (16 FMA + 2 MUL each), p' = r + beta p, x/r updates, two norms.
 CG_ITER_FP64_FLOPS_PER_SITE = 2 * 34 + 4 + 8 + 4 + 4
@@ -373,9 +375,9 @@ def run_ours(args, ws, rank, local):
     hbm, peak_kind = peaks()
     t_iter_ms = cg_ms / max(1, iters)
     achieved = CG_ITER_BYTES_PER_SITE * V / (t_iter_ms * 1e-3) / 1e9
-    # two kernels per CG iteration, an init and at most one early-exit pair per
-    # solve, four kernels per MD step, about 20 for the heatbath and the sums
-    launches = sum(2 * r.cg_iterations + 3 * r.cg_solves for r in res) + args.steps * (4 * W["nsteps"] + 20)
+    # one cooperative kernel per CG solve (the default, persistent solver), four
+    # kernels per MD step, about 20 for the heatbath and the sums
+    launches = sum(r.cg_solves for r in res) + args.steps * (4 * W["nsteps"] + 20)
 
     fp64_achieved = CG_ITER_FP64_FLOPS_PER_SITE * V / (t_iter_ms * 1e-3) / 1e12
     try:
@@ -393,18 +395,18 @@ def run_ours(args, ws, rank, local):
         "config": config_block(),
         "e2e": {"value": e2e_value, "unit": "trajectories/s", "h2d_bytes_per_step": 16 * V,
                 "d2h_bytes_per_step": 16 * V + 128},
-        "roofline": {"kernel": "CG iteration (k_cg1 + k_cg2_64), FP64", "bound": "hbm",
+        "roofline": {"kernel": "CG iteration inside k_pcg64 (persistent FP64 CG)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": peak_kind, "bytes_per_site": CG_ITER_BYTES_PER_SITE,
                      "ms_per_iteration": t_iter_ms,
                      "traffic": CG_ITER_DRAM_BYTES,
-                     "traffic_source": "profiles/cg_iteration_1024_fp64.md (ncu, one capture)",
-                     "note": "the FP64 CG kernels are bound by the FP64 pipe, not HBM: fp64_alu.frac is the "
+                     "traffic_source": "profiles/cg_iteration_1024_fp64_persistent.md (ncu, one capture)",
+                     "note": "the FP64 CG is bound by the FP64 pipe, not HBM: fp64_alu.frac is the "
                              "fraction of the measured FP64 FMA rate; dslash.at_2048.fp32_frac is the "
                              "HBM-bound FP32 stencil's"},
         "fp64_alu": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak, "peak_source": fp64_peak_kind,
                      "frac": fp64_achieved / fp64_peak, "flops_per_site": CG_ITER_FP64_FLOPS_PER_SITE,
-                     "note": "the FP64 CG kernels keep the FP64 pipe 85-89% busy (ncu); they are FP64-ALU-bound"},
+                     "note": "the FP64 CG keeps the FP64 pipe busy most of the time (ncu); it is FP64-ALU-bound"},
         "dslash": {"fp64_gbs": dslash_gbs, "fp64_ms_M": t_M, "fp64_ms_Mdag": t_Md, "fp64_frac": dslash_gbs / hbm,
                    "fp32_gbs": dslash32_gbs, "fp32_ms": t_M32, "bytes_per_site_fp64": 64, "bytes_per_site_fp32": 32,
                    "at_2048": dict(dslash_2048, fp64_frac=dslash_2048["fp64_gbs"] / hbm,

@@ -56,21 +56,47 @@ __device__ __forceinline__ bool grid_barrier(const GridBar& b) {
   return s_ok != 0;
 }
 
-// Grid total of v, the same value in every thread of every block.
-__device__ __forceinline__ bool grid_total(double v, double* part, const GridBar& bar, double& out) {
-  __shared__ double sh[kBlock / 32];
-  __shared__ double s_tot;
-  const double b = block_sum<kBlock, double>(v, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = b;
+// Grid total of the threads' partials v (added in their own precision within
+// a block, as the launch path's kernels do, and in FP64 across blocks, in index
+// order), handed to f, which runs in thread 0 of every block; every thread of
+// the block gets f's result.  The scalars that follow a sum (alpha, beta, the
+// stopping tests) are thus computed once per block: a double division is about
+// ten operations of the FP64 pipe, which retires two per SM per clock.
+template <typename T, class F>
+__device__ __forceinline__ bool grid_total_then(T v, double* part, const GridBar& bar, F f, decltype(f(0.0))& out) {
+  using S = decltype(f(0.0));
+  __shared__ T sh[kBlock / 32];
+  __shared__ double shd[kBlock / 32];
+  __shared__ S s_out;
+  const T b = block_sum<kBlock, T>(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = (double)b;
   if (!grid_barrier(bar)) return false;
   double s = 0;
   for (int i = threadIdx.x; i < (int)gridDim.x; i += kBlock) s += __ldcg(part + i);
-  s = block_sum<kBlock, double>(s, sh);
-  if (threadIdx.x == 0) s_tot = s;
+  s = block_sum<kBlock, double>(s, shd);
+  if (threadIdx.x == 0) s_out = f(s);
   __syncthreads();
-  out = s_tot;
+  out = s_out;
   return true;
 }
+
+__device__ __forceinline__ bool grid_total(double v, double* part, const GridBar& bar, double& out) {
+  return grid_total_then(v, part, bar, [](double t) { return t; }, out);
+}
+
+// What the iterations need after their sums.
+struct PcgStep64 {
+  double alpha, ax;  // x advances by ax p (alpha / m^2 in the unit-mass form)
+};
+struct PcgTail64 {
+  double rn, beta;
+  int status;  // -1: go on
+};
+struct PcgTailMx {
+  double rn;
+  float bf;
+  int need;  // a reliable update is due
+};
 
 __device__ __forceinline__ void pcg_report(CgState* st, CgLog* log, int log_index, double rr, double rr0, double stop,
                                            int iter, int n_ru, int status) {
@@ -145,13 +171,15 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
       va = fma(o.y, o.y, va);
     };
     stencil_ld<double, 0, MU0, UNIT>(g, a.km, ld_a, a.Wt, a.Wx, epi_a);
-    double pap;
-    if (!grid_total(va, partA, a.bar, pap)) {
+    PcgStep64 st;
+    if (!grid_total_then(va, partA, a.bar, [&](double pap) {
+          const double al = rr / pap;
+          return PcgStep64{al, UNIT ? al * a.inv_m2 : al};
+        }, st)) {
       status = TG_E_TIMEOUT;
       break;
     }
-    const double alpha = rr / pap;
-    const double ax = UNIT ? alpha * a.inv_m2 : alpha;
+    const double alpha = st.alpha, ax = st.ax;
     double vb = 0;
     auto ld_b = [&](int i) { return __ldcg(a.Mp + i); };
     auto epi_b = [&](int s, double2 ap, double2) {
@@ -166,18 +194,22 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
       vb = fma(rv.y, rv.y, vb);
     };
     stencil_ld<double, 1, MU0, UNIT>(g, a.kd, ld_b, a.Wt, a.Wx, epi_b);
-    double rn;
-    if (!grid_total(vb, partB, a.bar, rn)) {
+    PcgTail64 e;
+    if (!grid_total_then(vb, partB, a.bar, [&](double rn) {
+          PcgTail64 o{rn, rn / rr, -1};
+          if (isnan(rn)) o.status = TG_E_NAN;
+          else if (rn < stop) o.status = TG_OK;                // hmc.c:381
+          else if (rn / rr0 > 1e10) o.status = TG_E_DIVERGED;  // hmc.c:383-386
+          else if (iter + 1 >= a.maxiter) o.status = TG_E_NOCONV;
+          return o;
+        }, e)) {
       status = TG_E_TIMEOUT;
       break;
     }
     iter += 1;
-    beta = rn / rr;
-    rr = rn;
-    if (isnan(rn)) status = TG_E_NAN;
-    else if (rn < stop) status = TG_OK;                   // hmc.c:381
-    else if (rn / rr0 > 1e10) status = TG_E_DIVERGED;     // hmc.c:383-386
-    else if (iter >= a.maxiter) status = TG_E_NOCONV;
+    beta = e.beta;
+    rr = e.rn;
+    status = e.status;
     half ^= 1;
   }
   pcg_report(a.st, a.log, a.log_index, rr, rr0, stop, iter, 0, status);
@@ -213,12 +245,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
     if (isnan(rr)) status = TG_E_NAN;
     else if (!(rr >= stop) || rr == 0.0) status = TG_OK;
   }
-  double beta = 0;
+  float bf = 0.f;
   int half = 0;
   while (status < 0) {
     const float2* p_old = half ? a.p1 : a.p0;
     float2* p_new = half ? a.p0 : a.p1;
-    const float bf = (float)beta;
     float va = 0;
     auto ld_a = [&](int i) {
       const float2 rv = __ldcg(a.r + i), pv = __ldcg(p_old + i);
@@ -231,12 +262,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
       va = fmaf(o.y, o.y, va);
     };
     stencil_ld<float, 0, MU0>(g, a.km32, ld_a, a.Wt32, a.Wx32, epi_a);
-    double pap;
-    if (!grid_total((double)va, partA, a.bar, pap)) {
+    float af;
+    if (!grid_total_then(va, partA, a.bar, [&](double pap) { return (float)(rr / pap); }, af)) {
       status = TG_E_TIMEOUT;
       break;
     }
-    const float af = (float)(rr / pap);
     float vb = 0;
     auto ld_b = [&](int i) { return __ldcg(a.Mp + i); };
     auto epi_b = [&](int s, float2 ap, float2) {
@@ -251,19 +281,22 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
       vb = fmaf(rv.y, rv.y, vb);
     };
     stencil_ld<float, 1, MU0>(g, a.kd32, ld_b, a.Wt32, a.Wx32, epi_b);
-    double rn;
-    if (!grid_total((double)vb, partB, a.bar, rn)) {
+    PcgTailMx e;
+    if (!grid_total_then(vb, partB, a.bar, [&](double rn) {
+          PcgTailMx o{rn, (float)(rn / rr), 0};
+          o.need = since_ru + 1 >= a.ru_interval || rn < stop || rn < kRuDrop * rr_true || iter + 1 >= a.maxiter ||
+                   rn / rr0 > 1e10 || isnan(rn);
+          return o;
+        }, e)) {
       status = TG_E_TIMEOUT;
       break;
     }
     iter += 1;
     since_ru += 1;
-    beta = rn / rr;
-    rr = rn;
+    bf = e.bf;
+    rr = e.rn;
     half ^= 1;
-    const bool need = since_ru >= a.ru_interval || rn < stop || rn < kRuDrop * rr_true || iter >= a.maxiter ||
-                      rn / rr0 > 1e10 || isnan(rn);
-    if (!need) continue;
+    if (!e.need) continue;
     // reliable update: x += xs, xs = 0; r = b - M^dag M x in FP64; rs = (float) r
     TG_SITES(s, g.V) {
       const float2 d = __ldcg(a.xs + s);
@@ -299,7 +332,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
       status = TG_E_TIMEOUT;
       break;
     }
-    if (rt > kRuRestart * rr) beta = 0;  // the recursive residual was far too optimistic: restart p from r
+    if (rt > kRuRestart * rr) bf = 0.f;  // the recursive residual was far too optimistic: restart p from r
     rr_true = rt;
     rr = rt;
     since_ru = 0;

@@ -32,6 +32,8 @@ def main():
     ap.add_argument("--applies", type=int, default=20)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--graph", type=int, default=1)
+    ap.add_argument("--solver", choices=["default", "launches", "persistent"], default="default",
+                    help="CG scheduling: two launches per iteration, or one cooperative launch per solve")
     ap.add_argument("--batch", type=int, default=0, help="run the batched-chain case with this many chains")
     ap.add_argument("--trajectories", type=int, default=2)
     ap.add_argument("--sequential", type=int, default=0, help="chains to also run one at a time (FP64 path)")
@@ -63,7 +65,9 @@ def main():
         os.environ["TG_GRAPH"] = "1" if a.graph else "0"
         b = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
         prec = N.PREC_MIXED if a.precision == "mixed" else N.PREC_FP64
-        x, res = L.fmdm_invert_cg(b, cg_params(rel_tol=0.0, abs_tol2=0.0, maxiter=a.iters, precision=prec))
+        solver = {"default": N.SOLVER_DEFAULT, "launches": N.SOLVER_LAUNCHES, "persistent": N.SOLVER_PERSISTENT}
+        x, res = L.fmdm_invert_cg(b, cg_params(rel_tol=0.0, abs_tol2=0.0, maxiter=a.iters, precision=prec,
+                                               solver=solver[a.solver]))
         out["cg_iterations"] = res.iterations
         out["cg_status"] = N.STATUS_NAMES[res.status]
     L.close()
