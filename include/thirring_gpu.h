@@ -72,7 +72,8 @@ typedef struct {
 
 /* tg_cg_params.solver.  Both run the same iteration and stopping rules; they
  * differ in rounding of the grid sums only. */
-#define TG_SOLVER_DEFAULT 0     /* the faster of the two on this library's measurements       */
+#define TG_SOLVER_DEFAULT 0     /* the faster of the two on this library's measurements:
+                                   persistent (TG_SOLVER=launches|persistent overrides)    */
 #define TG_SOLVER_LAUNCHES 1    /* two kernel launches per iteration (graph WHILE node)       */
 #define TG_SOLVER_PERSISTENT 2  /* one cooperative launch per solve, grid barriers inside     */
 
@@ -93,7 +94,8 @@ typedef struct {
                               608-661, 698-699) -- it consumes V Gaussian pairs per
                               trajectory and vanishes identically at mu = 0              */
   int rng;                 /* TG_RNG_MT or TG_RNG_PHILOX for tg_trajectory                 */
-  int use_graph;           /* 1: run the trajectory as one CUDA graph (CG loops as
+  int use_graph;           /* 1: run the trajectory as one CUDA graph (a persistent
+                              solve is one node; launch-per-iteration CG loops are
                               conditional WHILE nodes); 0: eager launches              */
   unsigned long long seed; /* Philox key                                                  */
   tg_cg_params cg;         /* solver used inside the trajectory                           */
