@@ -278,7 +278,7 @@ bool use_persistent(const tg_cg_params& cp) {
 // arrival count is cleared first, so a solve that timed out leaves no trace.
 int enqueue_pcg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const double2* b, double2* x, int log_index) {
   const Links lk = links(L);
-  const GridBar bar{L->bar, L->bar + 1};
+  const GridBar bar{L->bar};
   TG_CK(cudaMemsetAsync(L->bar, 0, sizeof(unsigned), s));
   cudaError_t e;
   if (cp.precision == TG_PREC_MIXED) {

@@ -115,9 +115,8 @@ void lu_logdet(cudaStream_t s, int V, int nmat, double2* mats, double* out);
 // ---------------------------------------------------------------------------
 // Persistent CG (tg_pcg.cu): one cooperative launch per solve
 // ---------------------------------------------------------------------------
-struct GridBar {       // grid barrier: arrivals and generation (count must be 0 at launch)
+struct GridBar {       // grid barrier: monotonic arrival count (must be 0 at launch)
   unsigned* count;
-  unsigned* gen;
 };
 constexpr int kPcgMaxGrid = 4096;  // partial sums: 2 * kPcgMaxGrid doubles
 

@@ -24,30 +24,36 @@
 
 namespace tg {
 
-constexpr long long kBarrierSpinLimit = 1LL << 24;  // polls of >= 64 ns: over a second
+// polls of >= 32 ns plus an L2 round trip each: from about half a second to tens
+constexpr long long kBarrierSpinLimit = 1LL << 24;
 
+// The number of grid barriers this block has passed in this launch (thread 0
+// only; every block passes the same sequence of barriers).
+__device__ __forceinline__ unsigned& barrier_epoch() {
+  __shared__ unsigned epoch;
+  return epoch;
+}
+
+// Grid barrier on a monotonic arrival count (0 at launch): the k-th barrier is
+// passed once the count reaches k * gridDim.x.  Each block adds its arrival
+// without waiting for the atomic's result and polls the count, so no block
+// has to finish the barrier for the others.
 __device__ __forceinline__ bool grid_barrier(const GridBar& b) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned* vgen = b.gen;
-    const unsigned gen = *vgen;  // read before arriving: the last arrival bumps it
-    __threadfence();
-    const unsigned arrived = atomicAdd(b.count, 1u);
+    const unsigned target = (barrier_epoch() += 1) * gridDim.x;
+    __threadfence();  // the block's writes before its arrival
+    atomicAdd(b.count, 1u);
+    volatile unsigned* vcount = b.count;
     int ok = 1;
-    if (arrived == gridDim.x - 1) {
-      atomicExch(b.count, 0u);
-      __threadfence();
-      atomicAdd(b.gen, 1u);
-    } else {
-      long long spins = 0;
-      while (*vgen == gen) {
-        if (++spins > kBarrierSpinLimit) {
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
+    long long spins = 0;
+    while ((int)(*vcount - target) < 0) {
+      if (++spins > kBarrierSpinLimit) {
+        ok = 0;
+        break;
       }
+      __nanosleep(32);
     }
     __threadfence();
     s_ok = ok;
@@ -133,6 +139,7 @@ __device__ __forceinline__ double stop_of(double rr0, double rel_tol, double abs
 // ---------------------------------------------------------------------------
 template <bool MU0, bool UNIT>
 __global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
+  if (threadIdx.x == 0) barrier_epoch() = 0;
   const Geo& g = a.g;
   double* partA = a.part;
   double* partB = a.part + gridDim.x;
@@ -221,6 +228,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
 // ---------------------------------------------------------------------------
 template <bool MU0>
 __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
+  if (threadIdx.x == 0) barrier_epoch() = 0;
   const Geo& g = a.g;
   double* partA = a.part;
   double* partB = a.part + gridDim.x;
