@@ -385,6 +385,10 @@ def run_ours(args, ws, rank, local):
     except Exception:
         fp64_peak, fp64_peak_kind = FP64_PEAK_TFLOPS_NOMINAL, "nominal"
 
+    def fp64_peak_for_cap(hbm_gbs):
+        # the HBM fraction a CG iteration reaches when the FP64 pipe runs at its peak
+        return (fp64_peak * 1e12 / CG_ITER_FP64_FLOPS_PER_SITE * CG_ITER_BYTES_PER_SITE / 1e9) / hbm_gbs
+
     if rank != 0:
         return
     line = {
@@ -401,9 +405,10 @@ def run_ours(args, ws, rank, local):
                      "ms_per_iteration": t_iter_ms,
                      "traffic": CG_ITER_DRAM_BYTES,
                      "traffic_source": "profiles/cg_iteration_1024_fp64_persistent.md (ncu, one capture)",
-                     "note": "the FP64 CG is bound by the FP64 pipe, not HBM: fp64_alu.frac is the "
-                             "fraction of the measured FP64 FMA rate; dslash.at_2048.fp32_frac is the "
-                             "HBM-bound FP32 stencil's"},
+                     "note": "the FP64 CG is bound by the FP64 pipe, not HBM: at 88 flops per 208 B "
+                             "and the measured FP64 rate, the pipe caps this HBM fraction at "
+                             f"{fp64_peak_for_cap(hbm):.2f}; fp64_alu.frac is the fraction of the measured "
+                             "FP64 FMA rate; dslash.at_2048.fp32_frac is the HBM-bound FP32 stencil's"},
         "fp64_alu": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak, "peak_source": fp64_peak_kind,
                      "frac": fp64_achieved / fp64_peak, "flops_per_site": CG_ITER_FP64_FLOPS_PER_SITE,
                      "note": "the FP64 CG keeps the FP64 pipe busy most of the time (ncu); it is FP64-ALU-bound"},
