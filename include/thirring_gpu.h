@@ -331,6 +331,19 @@ int tg_batch_size(const tg_batch* B, int* nchains, long long* total_sites);
 /* gauge field of one chain: double[nt*nx*2] */
 int tg_batch_set_gauge(tg_batch* B, int chain, const double* A);
 int tg_batch_get_gauge(tg_batch* B, int chain, double* A);
+/* Checkpoint of a whole batch: every chain's parameters, its Philox trajectory
+ * counter, and the gauge fields.  Little-endian layout, byte offsets:
+ *   0 char[8] "TGBATCH1"   8 int32 version (1)   12 int32 nchains
+ *   16 int64 total sites
+ *   24 + 56 i: chain i -- int32 nt, nx, bc_t, bc_x; double m, g, mu;
+ *              uint64 seed, trajectory counter
+ *   24 + 56 nchains: double A[total sites * 2], the chains' fields concatenated
+ *   in chain order ([t][x][dir] each).
+ * Loading needs a batch created with the same chains (same order and
+ * parameters); a loaded batch continues bitwise as the saved one would. */
+size_t tg_batch_checkpoint_size(const tg_batch* B);
+int tg_batch_checkpoint_save(tg_batch* B, void* buf, size_t size);
+int tg_batch_checkpoint_load(tg_batch* B, const void* buf, size_t size);
 /* One trajectory of every chain; results[nchains] (cg_ms = device time of the
  * whole batch).  Returns the worst CG status over the chains. */
 int tg_batch_trajectory(tg_batch* B, const tg_batch_params* p, tg_traj_result* results);

@@ -75,3 +75,50 @@ def test_checkpoint_header_and_refusals(tg):
         L.restore(ck[:8] + struct.pack("<i", 2) + ck[12:])   # unknown version
     L.restore(ck)                                          # a good one still loads
     assert np.array_equal(L.get_gauge(), A)
+
+
+BATCH = [dict(nt=16, nx=16, m=0.3, g=0.5, mu=0.0, bc_t=-1, bc_x=1, seed=71),
+         dict(nt=32, nx=32, m=0.2, g=0.8, mu=0.1, bc_t=-1, bc_x=-1, seed=72),
+         dict(nt=24, nx=40, m=0.4, g=0.6, mu=0.0, bc_t=-1, bc_x=1, seed=73),
+         dict(nt=64, nx=64, m=0.25, g=0.7, mu=0.0, bc_t=-1, bc_x=1, seed=74)]
+
+
+def run_batch(tg, B, n):
+    bp = tg.batch_params(nsteps=6, block=51201, cg=tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=1))
+    out = []
+    for _ in range(n):
+        out.append([(r.dH, r.accepted, r.cg_iterations) for r in B.trajectory(bp)])
+    return out, [B.get_gauge(i) for i in range(len(BATCH))]
+
+
+def test_batch_resume_is_bitwise(tg, tmp_path):
+    rng = np.random.default_rng(8)
+    B = tg.Batch(BATCH)
+    for i, c in enumerate(BATCH):
+        B.set_gauge(i, rng.normal(0, 0.2, (c["nt"], c["nx"], 2)))
+    run_batch(tg, B, 2)
+    path = tmp_path / "batch.ckpt"
+    B.save(str(path))
+    sites = sum(c["nt"] * c["nx"] for c in BATCH)
+    assert path.stat().st_size == 24 + 56 * len(BATCH) + 16 * sites
+    want, A_want = run_batch(tg, B, 2)
+    B.close()
+
+    R = tg.Batch(BATCH)                          # fresh: fields 0, trajectory counters 0
+    R.load(str(path))
+    got, A_got = run_batch(tg, R, 2)
+    assert got == want
+    assert all(np.array_equal(a, b) for a, b in zip(A_got, A_want))
+    ck = R.checkpoint()
+    assert ck[:8] == b"TGBATCH1"
+    assert struct.unpack_from("<2iq", ck, 8) == (1, len(BATCH), sites)
+    assert [struct.unpack_from("<Q", ck, 24 + 56 * i + 48)[0] for i in range(len(BATCH))] == [4] * len(BATCH)
+    other = [dict(c) for c in BATCH]
+    other[2]["m"] = 0.41
+    with pytest.raises(tg.native.TGError):
+        tg.Batch(other).restore(ck)                   # another chain
+    with pytest.raises(tg.native.TGError):
+        tg.Batch(BATCH[:3]).restore(ck)               # another chain count
+    with pytest.raises(tg.native.TGError):
+        R.restore(ck[:-16])                           # truncated
+    R.close()

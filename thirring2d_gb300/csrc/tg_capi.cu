@@ -1640,6 +1640,84 @@ int tg_batch_get_gauge(tg_batch* B, int chain, double* A) {
   return TG_OK;
 }
 
+// ---- batch checkpoint --------------------------------------------------------
+namespace {
+constexpr char kBatchCkptMagic[8] = {'T', 'G', 'B', 'A', 'T', 'C', 'H', '1'};
+struct BatchCkptHeader {  // 24 bytes
+  char magic[8];
+  int32_t version, nchains;
+  int64_t total_sites;
+};
+struct BatchCkptChain {  // 56 bytes
+  int32_t nt, nx, bc_t, bc_x;
+  double m, g, mu;
+  uint64_t seed, traj;  // traj: the chain's Philox trajectory counter
+};
+size_t batch_ckpt_bytes(const tg_batch* B) {
+  return sizeof(BatchCkptHeader) + (size_t)B->n * sizeof(BatchCkptChain) + 2 * (size_t)B->total * sizeof(double);
+}
+int batch_download_results(tg_batch* B) {
+  TG_CK(cudaMemcpyAsync(B->h_res, B->d_res, sizeof(ChainResult) * B->n, cudaMemcpyDeviceToHost, B->stream));
+  TG_CK(cudaStreamSynchronize(B->stream));
+  return TG_OK;
+}
+}  // namespace
+
+size_t tg_batch_checkpoint_size(const tg_batch* B) { return B ? batch_ckpt_bytes(B) : 0; }
+
+int tg_batch_checkpoint_save(tg_batch* B, void* buf, size_t size) {
+  if (!B || !buf) return fail(TG_E_ARG, "null argument");
+  if (size < batch_ckpt_bytes(B)) return fail(TG_E_ARG, "checkpoint buffer too small");
+  TG_CK(cudaSetDevice(B->device));
+  TG_TRY(batch_download_results(B));
+  unsigned char* q = static_cast<unsigned char*>(buf);
+  BatchCkptHeader h{};
+  memcpy(h.magic, kBatchCkptMagic, 8);
+  h.version = 1;
+  h.nchains = B->n;
+  h.total_sites = B->total;
+  memcpy(q, &h, sizeof h);
+  q += sizeof h;
+  for (int i = 0; i < B->n; i++) {
+    const tg_chain_params& c = B->P[i];
+    BatchCkptChain e{c.nt, c.nx, c.bc_t, c.bc_x, c.m, c.g, c.mu, c.seed, B->h_res[i].traj};
+    memcpy(q, &e, sizeof e);
+    q += sizeof e;
+  }
+  TG_CK(cudaMemcpyAsync(q, B->F.A, sizeof(double2) * B->total, cudaMemcpyDeviceToHost, B->stream));
+  TG_CK(cudaStreamSynchronize(B->stream));
+  return TG_OK;
+}
+
+int tg_batch_checkpoint_load(tg_batch* B, const void* buf, size_t size) {
+  if (!B || !buf) return fail(TG_E_ARG, "null argument");
+  BatchCkptHeader h;
+  if (size < sizeof h) return fail(TG_E_ARG, "not a batch checkpoint");
+  memcpy(&h, buf, sizeof h);
+  if (memcmp(h.magic, kBatchCkptMagic, 8) != 0 || h.version != 1) return fail(TG_E_ARG, "not a batch checkpoint");
+  if (h.nchains != B->n || h.total_sites != B->total || size < batch_ckpt_bytes(B))
+    return fail(TG_E_ARG, "checkpoint of another batch (chain count or size)");
+  const unsigned char* q = static_cast<const unsigned char*>(buf) + sizeof h;
+  std::vector<uint64_t> traj(B->n);
+  for (int i = 0; i < B->n; i++) {
+    BatchCkptChain e;
+    memcpy(&e, q + i * sizeof e, sizeof e);
+    const tg_chain_params& c = B->P[i];
+    if (e.nt != c.nt || e.nx != c.nx || e.bc_t != c.bc_t || e.bc_x != c.bc_x || e.m != c.m || e.g != c.g ||
+        e.mu != c.mu || e.seed != c.seed)
+      return fail(TG_E_ARG, "checkpoint of another batch (chain " + std::to_string(i) + " differs)");
+    traj[i] = e.traj;
+  }
+  q += (size_t)B->n * sizeof(BatchCkptChain);
+  TG_CK(cudaSetDevice(B->device));
+  TG_TRY(batch_download_results(B));
+  for (int i = 0; i < B->n; i++) B->h_res[i].traj = traj[i];
+  TG_CK(cudaMemcpyAsync(B->d_res, B->h_res, sizeof(ChainResult) * B->n, cudaMemcpyHostToDevice, B->stream));
+  TG_CK(cudaMemcpyAsync(B->F.A, q, sizeof(double2) * B->total, cudaMemcpyHostToDevice, B->stream));
+  TG_CK(cudaStreamSynchronize(B->stream));
+  return TG_OK;
+}
+
 int tg_batch_trajectory(tg_batch* B, const tg_batch_params* p, tg_traj_result* results) {
   if (!B) return fail(TG_E_ARG, "null batch");
   TG_TRY(check_batch_params(p));

@@ -331,6 +331,26 @@ class Batch:
         N.check(self.lib.tg_batch_get_gauge(self.h, i, _p(A)))
         return A
 
+    # -- checkpoint and resume ------------------------------------------------
+    def checkpoint(self) -> bytes:
+        """Every chain's parameters, Philox trajectory counter and field, as bytes."""
+        n = self.lib.tg_batch_checkpoint_size(self.h)
+        buf = (C.c_ubyte * n)()
+        N.check(self.lib.tg_batch_checkpoint_save(self.h, buf, n))
+        return bytes(buf)
+
+    def restore(self, data: bytes):
+        buf = (C.c_ubyte * len(data)).from_buffer_copy(data)
+        N.check(self.lib.tg_batch_checkpoint_load(self.h, buf, len(data)))
+
+    def save(self, path: str):
+        with open(path, "wb") as f:
+            f.write(self.checkpoint())
+
+    def load(self, path: str):
+        with open(path, "rb") as f:
+            self.restore(f.read())
+
     def trajectory(self, bp: N.BatchParams | None = None):
         res = (N.TrajResult * self.n)()
         N.check(self.lib.tg_batch_trajectory(self.h, C.byref(bp or batch_params()), res), True)

@@ -104,6 +104,9 @@ SIGNATURES = {
     "tg_magnetisation": (C.c_int, [_vp, _dp]),
     "tg_fermion_phase": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "tg_chiral_condensate": (C.c_int, [_vp, C.POINTER(CgParams), C.c_int, C.c_ulonglong, _dp, _dp]),
+    "tg_batch_checkpoint_size": (C.c_size_t, [_vp]),
+    "tg_batch_checkpoint_save": (C.c_int, [_vp, _vp, C.c_size_t]),
+    "tg_batch_checkpoint_load": (C.c_int, [_vp, _vp, C.c_size_t]),
     "tg_checkpoint_size": (C.c_size_t, [_vp]),
     "tg_checkpoint_save": (C.c_int, [_vp, _vp, C.c_size_t]),
     "tg_checkpoint_load": (C.c_int, [_vp, _vp, C.c_size_t]),
