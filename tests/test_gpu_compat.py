@@ -71,3 +71,18 @@ def test_hmc_program_matches_oracle(oracle_lib, nt, nx, params):
     assert len(mags) == len(meas) == len(phases)
     for mg, ph, (wm, wp) in zip(mags, phases, meas):
         assert close(mg, wm, abs_=1e-6) and close(ph, wp, abs_=1e-5)
+
+
+def test_hmc_program_jsonl_log(tmp_path):
+    """HMC_JSONL appends one JSON line per trajectory; with HMC_VERBOSE=1 the
+    printed dS lines carry every digit and agree with the log exactly."""
+    import json
+    log = tmp_path / "traj.jsonl"
+    out = run_hmc("3 3 0.5 0.5 0.0 4242", 8, 8, {"HMC_JSONL": str(log), "HMC_VERBOSE": "1"})
+    rows = [json.loads(line) for line in log.read_text().splitlines()]
+    assert [r["trajectory"] for r in rows] == [1, 2, 3]
+    printed = [float(x) for x in re.findall(r"HMC End, dS ([-+0-9.eE]+),", out)]
+    decisions = re.findall(r"HMC (ACCEPTED|REJECTED)", out)
+    assert printed == [r["dH"] for r in rows]
+    assert decisions == ["ACCEPTED" if r["accepted"] else "REJECTED" for r in rows]
+    assert all(r["cg_solves"] == 11 and r["cg_iterations"] > 0 and r["cg_ms"] > 0 for r in rows)

@@ -343,6 +343,28 @@ void update_puregauge_hb(double*** a) {
   scatter_l(fd, a);
 }
 
+/* HMC_JSONL=<path>: one JSON line per trajectory appended to <path> (dH, the
+ * actions, the decision, CG work and device time). */
+static void log_trajectory(const tg_traj_result* r) {
+  static FILE* fp = NULL;
+  static int opened = 0;
+  static long n = 0;
+  if (!opened) {
+    opened = 1;
+    const char* path = getenv("HMC_JSONL");
+    if (path && *path) fp = fopen(path, "a");
+  }
+  if (!fp) return;
+  fprintf(fp,
+          "{\"trajectory\": %ld, \"dH\": %.17g, \"Sg0\": %.17g, \"Spf0\": %.17g, \"Smd0\": %.17g, "
+          "\"Smom0\": %.17g, \"Sg1\": %.17g, \"Spf1\": %.17g, \"Smd1\": %.17g, \"Smom1\": %.17g, "
+          "\"u\": %.17g, \"accepted\": %d, \"cg_solves\": %d, \"cg_iterations\": %d, "
+          "\"cg_max_iterations\": %d, \"reliable_updates\": %d, \"cg_ms\": %.6g}\n",
+          ++n, r->dH, r->Sg0, r->Spf0, r->Smd0, r->Smom0, r->Sg1, r->Spf1, r->Smd1, r->Smom1, r->u_accept,
+          r->accepted, r->cg_solves, r->cg_iterations, r->cg_max_iterations, r->reliable_updates, r->cg_ms);
+  fflush(fp);
+}
+
 /* update_gauge, hmc.c:671-746: the random fields are drawn here from the
  * shared stream in hmc.c's order (pseudofermion, momentum, noise, then the
  * accept uniform -- nothing else draws in between), the trajectory runs on
@@ -366,8 +388,14 @@ void update_gauge(double*** a) {
   tg_traj_result r;
   check(tg_trajectory_ext(L, &hp, f, f + 2 * V, f + 4 * V, u, &r), "tg_trajectory_ext");
   free(f);
-  printf("Start HMC: Sg %g, Smdm %g, Smd %g, Smom %g\n", r.Sg0, r.Spf0, r.Smd0, r.Smom0);
-  printf("HMC End, dS %g, Sg %g, Smdm %g, Smd %g, Sm %g\n", r.dH, r.Sg1, r.Spf1, r.Smd1, r.Smom1);
+  /* HMC_VERBOSE=1: the same lines with every digit (%.17g) */
+  const char* fmt0 = env_int("HMC_VERBOSE", 0) ? "Start HMC: Sg %.17g, Smdm %.17g, Smd %.17g, Smom %.17g\n"
+                                               : "Start HMC: Sg %g, Smdm %g, Smd %g, Smom %g\n";
+  const char* fmt1 = env_int("HMC_VERBOSE", 0) ? "HMC End, dS %.17g, Sg %.17g, Smdm %.17g, Smd %.17g, Sm %.17g\n"
+                                               : "HMC End, dS %g, Sg %g, Smdm %g, Smd %g, Sm %g\n";
+  printf(fmt0, r.Sg0, r.Spf0, r.Smd0, r.Smom0);
+  printf(fmt1, r.dH, r.Sg1, r.Spf1, r.Smd1, r.Smom1);
+  log_trajectory(&r);
   if (r.accepted) {
     printf("HMC ACCEPTED\n");
     if (tg_get_gauge(L, fd) != TG_OK) fatal("tg_get_gauge");
