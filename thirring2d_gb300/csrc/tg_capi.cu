@@ -7,6 +7,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -137,6 +139,15 @@ struct tg_lattice {
 };
 
 namespace {
+
+// NVTX range for the lifetime of a scope: the host side of an entry point or
+// a trajectory phase, for Nsight timelines (no cost without a tool attached).
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range&) = delete;
+  Range& operator=(const Range&) = delete;
+};
 
 OpK<double> op_k(const tg_lattice* L, int dagger) {
   double ep = exp(L->P.mu), em = exp(-L->P.mu);
@@ -521,29 +532,33 @@ int enqueue_trajectory(tg_lattice* L, cudaStream_t s, const tg_hmc_params& p, bo
     solve++;
     return TG_OK;
   };
-  if (p.rng == TG_RNG_PHILOX) {
-    for (int k = 0; k < p.npf; k++) philox_gauss(s, g, p.seed, ts, (unsigned)k, L->eta + (size_t)k * V);
-    philox_gauss(s, g, p.seed, ts, 16u, L->mom);
-    if (use_noise) philox_gauss(s, g, p.seed, ts, 17u, L->noise);
-    philox_uniform(s, p.seed, ts, 18u);
+  {  // heatbath and start actions
+    Range range("heatbath");
+    if (p.rng == TG_RNG_PHILOX) {
+      for (int k = 0; k < p.npf; k++) philox_gauss(s, g, p.seed, ts, (unsigned)k, L->eta + (size_t)k * V);
+      philox_gauss(s, g, p.seed, ts, 16u, L->mom);
+      if (use_noise) philox_gauss(s, g, p.seed, ts, 17u, L->noise);
+      philox_uniform(s, p.seed, ts, 18u);
+    }
+    link_phase(s, g, L->P.bc_t, L->P.bc_x, L->A, link_out(L));
+    // start: S_pf = |eta|^2 exactly (phi = M^dag eta), hmc.c:418-436
+    TG_CK(cudaMemsetAsync(&ts->Spf0, 0, sizeof(double), s));
+    for (int k = 0; k < p.npf; k++) {
+      norm2(s, g, L->eta + (size_t)k * V, &ts->Spf0, 1, L->red);
+      dslash64(s, g, kd, 1, L->eta + (size_t)k * V, L->phi + (size_t)k * V, L->Wt, L->Wx);
+    }
+    norm2(s, g, L->mom, &ts->Smom0, 0, L->red);
+    gauge_action(s, g, L->A, kNf / L->P.g, &ts->Sg0, L->red);
+    if (use_noise) md_action(s, g, kd, L->noise, L->Wt, L->Wx, &ts->Smd0, L->red);
+    else TG_CK(cudaMemsetAsync(&ts->Smd0, 0, sizeof(double), s));
+    TG_CK(cudaMemcpyAsync(L->Anew, L->A, (size_t)V * sizeof(double2), cudaMemcpyDeviceToDevice, s));
   }
-  link_phase(s, g, L->P.bc_t, L->P.bc_x, L->A, link_out(L));
-  // start: S_pf = |eta|^2 exactly (phi = M^dag eta), hmc.c:418-436
-  TG_CK(cudaMemsetAsync(&ts->Spf0, 0, sizeof(double), s));
-  for (int k = 0; k < p.npf; k++) {
-    norm2(s, g, L->eta + (size_t)k * V, &ts->Spf0, 1, L->red);
-    dslash64(s, g, kd, 1, L->eta + (size_t)k * V, L->phi + (size_t)k * V, L->Wt, L->Wx);
-  }
-  norm2(s, g, L->mom, &ts->Smom0, 0, L->red);
-  gauge_action(s, g, L->A, kNf / L->P.g, &ts->Sg0, L->red);
-  if (use_noise) md_action(s, g, kd, L->noise, L->Wt, L->Wx, &ts->Smd0, L->red);
-  else TG_CK(cudaMemsetAsync(&ts->Smd0, 0, sizeof(double), s));
-  TG_CK(cudaMemcpyAsync(L->Anew, L->A, (size_t)V * sizeof(double2), cudaMemcpyDeviceToDevice, s));
   // leapfrog, hmc.c:708-716; the two half steps between MD steps share a launch
   const double eps = p.tau / p.nsteps;
   const double c = 2.0 * (p.tau * 0.5 / p.nsteps);
   const double gfac = eps * kNf / L->P.g;
   for (int i = 0; i < p.nsteps; i++) {
+    Range step("md_step");
     gauge_step(s, g, L->P.bc_t, L->P.bc_x, L->Anew, L->mom, c, i == 0 ? 1 : 2, link_out(L));
     if (p.npf == 0)
       momentum_update(s, g, L->P.bc_t, L->P.bc_x, ep, em, L->Anew, L->Wt, L->Wx, nullptr, nullptr, L->noise, L->mom, eps, gfac,
@@ -555,6 +570,7 @@ int enqueue_trajectory(tg_lattice* L, cudaStream_t s, const tg_hmc_params& p, bo
       momentum_update(s, g, L->P.bc_t, L->P.bc_x, ep, em, L->Anew, L->Wt, L->Wx, L->chi, L->Mchi, L->noise, L->mom, eps, gfac, flags);
     }
   }
+  Range end("end_actions");
   gauge_step(s, g, L->P.bc_t, L->P.bc_x, L->Anew, L->mom, c, 1, link_out(L));
   // end actions, hmc.c:719-726
   TG_CK(cudaMemsetAsync(&ts->Spf1, 0, sizeof(double), s));
@@ -582,6 +598,7 @@ int check_hmc_params(const tg_hmc_params* p) {
 }
 
 int run_trajectory(tg_lattice* L, const tg_hmc_params& p, tg_traj_result* r) {
+  Range range("tg_trajectory");
   TG_TRY(ensure_pf(L, p.npf > 0 ? p.npf : 1));
   const int nsolves = (p.nsteps + 1) * p.npf;
   TG_TRY(ensure_events(L, 2 * (size_t)nsolves + 2));
@@ -876,6 +893,7 @@ int tg_time_apply(tg_lattice* L, int n, int dagger, int precision, double* ms_pe
 }
 
 int tg_cg(tg_lattice* L, const tg_cg_params* cp, const double* b, double* x, tg_cg_result* res) {
+  Range range("tg_cg");
   if (!L || !b || !x) return fail(TG_E_ARG, "null argument");
   TG_TRY(check_cg_params(cp));
   TG_TRY(upload(L, L->vin, b, 2 * (size_t)L->V));
@@ -1719,6 +1737,7 @@ int tg_batch_checkpoint_load(tg_batch* B, const void* buf, size_t size) {
 }
 
 int tg_batch_trajectory(tg_batch* B, const tg_batch_params* p, tg_traj_result* results) {
+  Range range("tg_batch_trajectory");
   if (!B) return fail(TG_E_ARG, "null batch");
   TG_TRY(check_batch_params(p));
   TG_CK(cudaSetDevice(B->device));
