@@ -166,7 +166,7 @@ OpK<float> op_k32(const tg_lattice* L, int dagger) {
 }
 // TG_SOLVER_DEFAULT: the persistent solver (one cooperative launch per solve),
 // measured faster than two launches per iteration on the 1024^2 trajectory:
-// FP64 1.396 vs 1.338, mixed 5.40 vs 4.25 trajectories/s
+// FP64 1.416 vs 1.342, mixed 5.56 vs 4.33 trajectories/s
 constexpr bool kDefaultPersistent = true;
 
 // The FP64 CG runs in unit-mass form (links W / m) whenever 1/m is a finite

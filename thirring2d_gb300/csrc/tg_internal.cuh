@@ -162,7 +162,8 @@ inline int grid_of(const Geo& g) { return g.grid; }
 inline int stream_grid(int n) { return nblocks(n); }  // streaming kernels without reductions
 
 // grid-stride loop over the sites of a kernel
-#define TG_SITES(s, n) for (int s = blockIdx.x * kBlock + threadIdx.x; s < (n); s += gridDim.x * kBlock)
+#define TG_SITES(s, n) \
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < (n); s += gridDim.x * blockDim.x)
 
 // ---------------------------------------------------------------------------
 // Device state of one CG solve.  Lives in device memory; all the scalar

@@ -27,6 +27,11 @@ namespace tg {
 // polls of >= 32 ns plus an L2 round trip each: from about half a second to tens
 constexpr long long kBarrierSpinLimit = 1LL << 24;
 
+// Threads per block and blocks per SM of the persistent kernels: fewer, larger
+// blocks meet at each grid barrier with fewer arrivals.
+constexpr int kPcgBlock = 512;
+constexpr int kPcgBlocksPerSM = 1;
+
 // The number of grid barriers this block has passed in this launch (thread 0
 // only; every block passes the same sequence of barriers).
 __device__ __forceinline__ unsigned& barrier_epoch() {
@@ -68,26 +73,27 @@ __device__ __forceinline__ bool grid_barrier(const GridBar& b) {
 // the block gets f's result.  The scalars that follow a sum (alpha, beta, the
 // stopping tests) are thus computed once per block: a double division is about
 // ten operations of the FP64 pipe, which retires two per SM per clock.
-template <typename T, class F>
+template <int BS, typename T, class F>
 __device__ __forceinline__ bool grid_total_then(T v, double* part, const GridBar& bar, F f, decltype(f(0.0))& out) {
   using S = decltype(f(0.0));
-  __shared__ T sh[kBlock / 32];
-  __shared__ double shd[kBlock / 32];
+  __shared__ T sh[BS / 32];
+  __shared__ double shd[BS / 32];
   __shared__ S s_out;
-  const T b = block_sum<kBlock, T>(v, sh);
+  const T b = block_sum<BS, T>(v, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = (double)b;
   if (!grid_barrier(bar)) return false;
   double s = 0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += kBlock) s += __ldcg(part + i);
-  s = block_sum<kBlock, double>(s, shd);
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += BS) s += __ldcg(part + i);
+  s = block_sum<BS, double>(s, shd);
   if (threadIdx.x == 0) s_out = f(s);
   __syncthreads();
   out = s_out;
   return true;
 }
 
+template <int BS>
 __device__ __forceinline__ bool grid_total(double v, double* part, const GridBar& bar, double& out) {
-  return grid_total_then(v, part, bar, [](double t) { return t; }, out);
+  return grid_total_then<BS>(v, part, bar, [](double t) { return t; }, out);
 }
 
 // What the iterations need after their sums.
@@ -138,7 +144,8 @@ __device__ __forceinline__ double stop_of(double rr0, double rel_tol, double abs
 // FP64: the iteration of k_cg1 + k_cg2_64 (unit-mass form when UNIT)
 // ---------------------------------------------------------------------------
 template <bool MU0, bool UNIT>
-__global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
+__global__ void __launch_bounds__(kPcgBlock, kPcgBlocksPerSM) k_pcg64(Pcg64Args a) {
+  constexpr int BS = kPcgBlock;
   if (threadIdx.x == 0) barrier_epoch() = 0;
   const Geo& g = a.g;
   double* partA = a.part;
@@ -154,7 +161,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
   }
   double rr = 0;
   int status = -1, iter = 0;
-  if (!grid_total(v, partB, a.bar, rr)) status = TG_E_TIMEOUT;
+  if (!grid_total<BS>(v, partB, a.bar, rr)) status = TG_E_TIMEOUT;
   const double rr0 = rr;
   const double stop = stop_of(rr0, a.rel_tol, a.abs_tol2);
   if (status < 0) {
@@ -179,7 +186,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
     };
     stencil_ld<double, 0, MU0, UNIT>(g, a.km, ld_a, a.Wt, a.Wx, epi_a);
     PcgStep64 st;
-    if (!grid_total_then(va, partA, a.bar, [&](double pap) {
+    if (!grid_total_then<BS>(va, partA, a.bar, [&](double pap) {
           const double al = rr / pap;
           return PcgStep64{al, UNIT ? al * a.inv_m2 : al};
         }, st)) {
@@ -202,7 +209,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
     };
     stencil_ld<double, 1, MU0, UNIT>(g, a.kd, ld_b, a.Wt, a.Wx, epi_b);
     PcgTail64 e;
-    if (!grid_total_then(vb, partB, a.bar, [&](double rn) {
+    if (!grid_total_then<BS>(vb, partB, a.bar, [&](double rn) {
           PcgTail64 o{rn, rn / rr, -1};
           if (isnan(rn)) o.status = TG_E_NAN;
           else if (rn < stop) o.status = TG_OK;                // hmc.c:381
@@ -227,7 +234,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcg64(Pcg64Args a) {
 // k_ru1..3 with the same triggers and restart rule.
 // ---------------------------------------------------------------------------
 template <bool MU0>
-__global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
+__global__ void __launch_bounds__(kPcgBlock, kPcgBlocksPerSM) k_pcgmx(PcgMxArgs a) {
+  constexpr int BS = kPcgBlock;
   if (threadIdx.x == 0) barrier_epoch() = 0;
   const Geo& g = a.g;
   double* partA = a.part;
@@ -245,7 +253,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
   }
   double rr = 0;
   int status = -1, iter = 0, n_ru = 0, since_ru = 0;
-  if (!grid_total(v, partB, a.bar, rr)) status = TG_E_TIMEOUT;
+  if (!grid_total<BS>(v, partB, a.bar, rr)) status = TG_E_TIMEOUT;
   const double rr0 = rr;
   const double stop = stop_of(rr0, a.rel_tol, a.abs_tol2);
   double rr_true = rr;
@@ -271,7 +279,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
     };
     stencil_ld<float, 0, MU0>(g, a.km32, ld_a, a.Wt32, a.Wx32, epi_a);
     float af;
-    if (!grid_total_then(va, partA, a.bar, [&](double pap) { return (float)(rr / pap); }, af)) {
+    if (!grid_total_then<BS>(va, partA, a.bar, [&](double pap) { return (float)(rr / pap); }, af)) {
       status = TG_E_TIMEOUT;
       break;
     }
@@ -290,7 +298,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
     };
     stencil_ld<float, 1, MU0>(g, a.kd32, ld_b, a.Wt32, a.Wx32, epi_b);
     PcgTailMx e;
-    if (!grid_total_then(vb, partB, a.bar, [&](double rn) {
+    if (!grid_total_then<BS>(vb, partB, a.bar, [&](double rn) {
           PcgTailMx o{rn, (float)(rn / rr), 0};
           o.need = since_ru + 1 >= a.ru_interval || rn < stop || rn < kRuDrop * rr_true || iter + 1 >= a.maxiter ||
                    rn / rr0 > 1e10 || isnan(rn);
@@ -336,7 +344,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
     };
     stencil_ld<double, 1, MU0>(g, a.kd, ld_t, a.Wt, a.Wx, epi_t);
     double rt;
-    if (!grid_total(vt, partA, a.bar, rt)) {
+    if (!grid_total<BS>(vt, partA, a.bar, rt)) {
       status = TG_E_TIMEOUT;
       break;
     }
@@ -354,7 +362,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_pcgmx(PcgMxArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Launchers: grid = co-resident blocks (2 per SM at 256 threads), at most the
+// Launchers: grid = co-resident blocks (kPcgBlocksPerSM per SM), at most the
 // stencil's work; cooperative launch so the barrier cannot wait on a block
 // that is not running.
 // ---------------------------------------------------------------------------
@@ -367,7 +375,7 @@ template <class K> int pcg_resident(K kernel) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm <= 0)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPcgBlock, 0) != cudaSuccess || per_sm <= 0)
     per_sm = 1;
   const int n = per_sm * sms;
   cache.emplace((const void*)kernel, n);
@@ -377,7 +385,7 @@ template <class K> int pcg_resident(K kernel) {
 template <class K, class Args> cudaError_t coop_launch(K kernel, int grid, cudaStream_t s, const Args& a) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(kBlock);
+  cfg.blockDim = dim3(kPcgBlock);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -389,8 +397,8 @@ template <class K, class Args> cudaError_t coop_launch(K kernel, int grid, cudaS
 }
 
 int pcg_grid(const Geo& g, int resident) {
-  const int work = g.march ? ((g.nx >> 5) * ((g.nt + kMarchT - 1) / kMarchT) + kBlock / 32 - 1) / (kBlock / 32)
-                           : nblocks(g.V);
+  const int work = g.march ? ((g.nx >> 5) * ((g.nt + kMarchT - 1) / kMarchT) + kPcgBlock / 32 - 1) / (kPcgBlock / 32)
+                           : nblocks(g.V, kPcgBlock);
   int grid = resident < work ? resident : work;
   if (grid > kPcgMaxGrid) grid = kPcgMaxGrid;
   return grid > 0 ? grid : 1;

@@ -116,7 +116,7 @@ __device__ __forceinline__ void march_segment(const Geo& g, const OpK<R>& k, Ld&
 // restarts its march only where its range crosses into a new strip.  Calls
 // f(xw, ta, tb) for each strip segment of this warp's range.
 template <class F> __device__ __forceinline__ void for_warp_rows(const Geo& g, F&& f) {
-  constexpr int wpb = kBlock / 32;
+  const int wpb = (int)(blockDim.x >> 5);
   const long long rows = (long long)(g.nx >> 5) * g.nt;
   const long long nw = (long long)gridDim.x * wpb;
   const long long gw = (long long)blockIdx.x * wpb + (threadIdx.x >> 5);
