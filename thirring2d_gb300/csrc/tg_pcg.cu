@@ -17,6 +17,8 @@
 // its next barrier, so a fault in the scheme cannot hang the GPU.
 #include <math.h>
 
+#include <algorithm>
+
 #include <mutex>
 #include <unordered_map>
 
@@ -27,10 +29,12 @@ namespace tg {
 // polls of >= 32 ns plus an L2 round trip each: from about half a second to tens
 constexpr long long kBarrierSpinLimit = 1LL << 24;
 
-// Threads per block and blocks per SM of the persistent kernels: fewer, larger
-// blocks meet at each grid barrier with fewer arrivals.
-constexpr int kPcgBlock = 512;
-constexpr int kPcgBlocksPerSM = 1;
+// Threads per block of the persistent kernels (512 / BS blocks per SM, 128
+// registers): one block of 512 threads per SM on lattices that fill the GPU --
+// fewer arrivals at each grid barrier -- and two of 256 on smaller ones, whose
+// march work (at least kMarchT rows per warp) would otherwise occupy too few
+// SMs.
+constexpr int pcg_min_blocks(int bs) { return 512 / bs; }
 
 // The number of grid barriers this block has passed in this launch (thread 0
 // only; every block passes the same sequence of barriers).
@@ -143,9 +147,8 @@ __device__ __forceinline__ double stop_of(double rr0, double rel_tol, double abs
 // ---------------------------------------------------------------------------
 // FP64: the iteration of k_cg1 + k_cg2_64 (unit-mass form when UNIT)
 // ---------------------------------------------------------------------------
-template <bool MU0, bool UNIT>
-__global__ void __launch_bounds__(kPcgBlock, kPcgBlocksPerSM) k_pcg64(Pcg64Args a) {
-  constexpr int BS = kPcgBlock;
+template <int BS, bool MU0, bool UNIT>
+__global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcg64(Pcg64Args a) {
   if (threadIdx.x == 0) barrier_epoch() = 0;
   const Geo& g = a.g;
   double* partA = a.part;
@@ -233,9 +236,8 @@ __global__ void __launch_bounds__(kPcgBlock, kPcgBlocksPerSM) k_pcg64(Pcg64Args 
 // Mixed: the iteration of k_cg1<float> + k_cgmx2, and the reliable update of
 // k_ru1..3 with the same triggers and restart rule.
 // ---------------------------------------------------------------------------
-template <bool MU0>
-__global__ void __launch_bounds__(kPcgBlock, kPcgBlocksPerSM) k_pcgmx(PcgMxArgs a) {
-  constexpr int BS = kPcgBlock;
+template <int BS, bool MU0>
+__global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
   if (threadIdx.x == 0) barrier_epoch() = 0;
   const Geo& g = a.g;
   double* partA = a.part;
@@ -362,11 +364,11 @@ __global__ void __launch_bounds__(kPcgBlock, kPcgBlocksPerSM) k_pcgmx(PcgMxArgs 
 }
 
 // ---------------------------------------------------------------------------
-// Launchers: grid = co-resident blocks (kPcgBlocksPerSM per SM), at most the
+// Launchers: grid = co-resident blocks, at most the
 // stencil's work; cooperative launch so the barrier cannot wait on a block
 // that is not running.
 // ---------------------------------------------------------------------------
-template <class K> int pcg_resident(K kernel) {
+template <class K> int pcg_resident(K kernel, int bs) {
   static std::mutex mu;
   static std::unordered_map<const void*, int> cache;
   std::lock_guard<std::mutex> lock(mu);
@@ -375,17 +377,17 @@ template <class K> int pcg_resident(K kernel) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPcgBlock, 0) != cudaSuccess || per_sm <= 0)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, bs, 0) != cudaSuccess || per_sm <= 0)
     per_sm = 1;
   const int n = per_sm * sms;
   cache.emplace((const void*)kernel, n);
   return n;
 }
 
-template <class K, class Args> cudaError_t coop_launch(K kernel, int grid, cudaStream_t s, const Args& a) {
+template <class K, class Args> cudaError_t coop_launch(K kernel, int grid, int bs, cudaStream_t s, const Args& a) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(kPcgBlock);
+  cfg.blockDim = dim3((unsigned)bs);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -396,24 +398,38 @@ template <class K, class Args> cudaError_t coop_launch(K kernel, int grid, cudaS
   return cudaLaunchKernelEx(&cfg, kernel, a);
 }
 
-int pcg_grid(const Geo& g, int resident) {
-  const int work = g.march ? ((g.nx >> 5) * ((g.nt + kMarchT - 1) / kMarchT) + kPcgBlock / 32 - 1) / (kPcgBlock / 32)
-                           : nblocks(g.V, kPcgBlock);
-  int grid = resident < work ? resident : work;
+// blocks of bs threads the stencil can use: at least kMarchT rows per warp
+int pcg_work(const Geo& g, int bs) {
+  return g.march ? ((g.nx >> 5) * ((g.nt + kMarchT - 1) / kMarchT) + bs / 32 - 1) / (bs / 32) : nblocks(g.V, bs);
+}
+
+int pcg_grid(const Geo& g, int resident, int bs) {
+  int grid = std::min(resident, pcg_work(g, bs));
   if (grid > kPcgMaxGrid) grid = kPcgMaxGrid;
   return grid > 0 ? grid : 1;
 }
 
+// the 512-thread kernel when its blocks fill every SM, else the 256-thread one
+template <class K512, class K256, class Args>
+cudaError_t pcg_launch(const Geo& g, K512 k512, K256 k256, cudaStream_t s, const Args& a) {
+  const int r512 = pcg_resident(k512, 512);
+  if (pcg_work(g, 512) >= r512) return coop_launch(k512, pcg_grid(g, r512, 512), 512, s, a);
+  return coop_launch(k256, pcg_grid(g, pcg_resident(k256, 256), 256), 256, s, a);
+}
+
 cudaError_t pcg64(cudaStream_t s, bool mu0, Pcg64Args a) {
   const bool unit = a.inv_m2 != 0.0;
-  auto k = mu0 ? (unit ? k_pcg64<true, true> : k_pcg64<true, false>)
-               : (unit ? k_pcg64<false, true> : k_pcg64<false, false>);
-  return coop_launch(k, pcg_grid(a.g, pcg_resident(k)), s, a);
+  if (mu0) {
+    if (unit) return pcg_launch(a.g, k_pcg64<512, true, true>, k_pcg64<256, true, true>, s, a);
+    return pcg_launch(a.g, k_pcg64<512, true, false>, k_pcg64<256, true, false>, s, a);
+  }
+  if (unit) return pcg_launch(a.g, k_pcg64<512, false, true>, k_pcg64<256, false, true>, s, a);
+  return pcg_launch(a.g, k_pcg64<512, false, false>, k_pcg64<256, false, false>, s, a);
 }
 
 cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a) {
-  auto k = mu0 ? k_pcgmx<true> : k_pcgmx<false>;
-  return coop_launch(k, pcg_grid(a.g, pcg_resident(k)), s, a);
+  if (mu0) return pcg_launch(a.g, k_pcgmx<512, true>, k_pcgmx<256, true>, s, a);
+  return pcg_launch(a.g, k_pcgmx<512, false>, k_pcgmx<256, false>, s, a);
 }
 
 }  // namespace tg
