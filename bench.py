@@ -64,7 +64,7 @@ def peaks():
 # DRAM bytes (read + write) of one FP64 CG iteration of the persistent solver
 # (k_pcg64, 100 iterations in one launch) at 1024^2 from one ncu capture:
 # profiles/cg_iteration_1024_fp64_persistent.md.
-CG_ITER_DRAM_BYTES = 120.8e6
+CG_ITER_DRAM_BYTES = 116.4e6
 # FP64 work of one CG iteration per site, in flops (FMA = 2): two operator
 # applies (16 FMA + 2 MUL each), p' = r + beta p, x/r updates, two norms.
 CG_ITER_FP64_FLOPS_PER_SITE = 2 * 34 + 4 + 8 + 4 + 4
