@@ -236,6 +236,12 @@ int tg_measure_fp64_peak(int device, double* tflops);
  * bounded wait on a TMA copy ran out) since the library was loaded: 0 in a
  * healthy run.  No reference counterpart. */
 int tg_stage_faults(int device, unsigned* count);
+/* The persistent solver's grid barrier on its failure path: one barrier on a
+ * small cooperative grid that also waits for phantom_blocks blocks that do not
+ * exist.  *status = TG_OK when it was passed (phantom_blocks = 0), TG_E_TIMEOUT
+ * when it gave up after its bounded wait (tens of milliseconds); the device
+ * stays usable either way.  No reference counterpart. */
+int tg_grid_barrier_check(int device, int phantom_blocks, int* status);
 
 /* ---- fermion-bag propagator matrix ----------------------------------------- */
 /* calc_Dinv with WITH_MASS_MONOMERS (fermion_matrix.c:189-351): for every

@@ -130,3 +130,23 @@ def test_persistent_mixed_trajectory(tg):
         assert abs(r.dH - want[0]) < 1e-9
         assert r.accepted == int(want[9])
         assert r.reliable_updates > 0
+
+
+def test_grid_barrier_gives_up_and_device_stays_usable(tg):
+    """The grid barrier's bounded wait: a barrier that also waits for blocks
+    that never arrive returns TG_E_TIMEOUT after its poll limit instead of
+    hanging, and the device keeps working (a solve right after converges)."""
+    import ctypes as C
+    lib = tg.native.load()
+    st = C.c_int(-99)
+    tg.native.check(lib.tg_grid_barrier_check(0, 0, C.byref(st)))
+    assert st.value == 0
+    tg.native.check(lib.tg_grid_barrier_check(0, 1, C.byref(st)))
+    assert st.value == tg.native.TG_E_TIMEOUT
+    L = tg.Lattice(32, 32, 0.2, 0.5, 0.0, -1, 1)
+    L.set_gauge(np.random.default_rng(4).normal(0, 0.3, (32, 32, 2)))
+    b = np.random.default_rng(5).normal(size=(32, 32)) + 0j
+    x, res = L.fmdm_invert_cg(b, tg.cg_params(rel_tol=1e-10, abs_tol2=0, solver=tg.native.SOLVER_PERSISTENT))
+    assert res.status == 0
+    r = b - L.fm_conjugate_mul(L.fm_mul(x))
+    assert np.linalg.norm(r) < 2e-10 * np.linalg.norm(b)

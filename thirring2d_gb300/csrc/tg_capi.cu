@@ -654,6 +654,28 @@ extern "C" {
 const char* tg_last_error(void) { return g_err.c_str(); }
 const char* tg_version(void) { return "thirring2d_gb300 0.1 (sm_103a)"; }
 
+int tg_grid_barrier_check(int device, int phantom_blocks, int* status) {
+  if (!status || phantom_blocks < 0) return fail(TG_E_ARG, "bad argument");
+  TG_CK(cudaSetDevice(device));
+  unsigned* count = nullptr;
+  int* st = nullptr;
+  TG_TRY(dmalloc(&count, 1));
+  if (dmalloc(&st, 1) != TG_OK) {
+    cudaFree(count);
+    return TG_E_ALLOC;
+  }
+  cudaError_t e = cudaMemset(count, 0, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(st, 0xff, sizeof(int));
+  // 2^16 polls: tens of milliseconds before a barrier that cannot complete gives up
+  if (e == cudaSuccess) e = barrier_check(0, count, (unsigned)phantom_blocks, 1LL << 16, st);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(status, st, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(count);
+  cudaFree(st);
+  if (e != cudaSuccess) return fail(TG_E_CUDA, std::string("barrier check: ") + cudaGetErrorString(e));
+  return TG_OK;
+}
+
 int tg_stage_faults(int device, unsigned* count) {
   if (!count) return fail(TG_E_ARG, "null argument");
   TG_CK(cudaSetDevice(device));

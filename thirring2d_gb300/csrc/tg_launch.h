@@ -156,6 +156,9 @@ struct PcgMxArgs {
 
 cudaError_t pcg64(cudaStream_t s, bool mu0, Pcg64Args a);
 cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a);
+// one grid barrier (4 blocks, cooperative) that also waits for `phantom` absent
+// blocks, giving up after `limit` polls: *status = TG_OK or TG_E_TIMEOUT
+cudaError_t barrier_check(cudaStream_t s, unsigned* count, unsigned phantom, long long limit, int* status);
 
 // staged-kernel waits (tg_kernels.cu) that ran out since the library was loaded
 unsigned stage_faults();

@@ -44,21 +44,22 @@ __device__ __forceinline__ unsigned& barrier_epoch() {
 }
 
 // Grid barrier on a monotonic arrival count (0 at launch): the k-th barrier is
-// passed once the count reaches k * gridDim.x.  Each block adds its arrival
-// without waiting for the atomic's result and polls the count, so no block
-// has to finish the barrier for the others.
-__device__ __forceinline__ bool grid_barrier(const GridBar& b) {
+// passed once the count reaches k * nblocks (the grid's blocks).  Each block
+// adds its arrival without waiting for the atomic's result and polls the
+// count, so no block has to finish the barrier for the others.  After `limit`
+// polls a block gives up and returns false.
+__device__ __forceinline__ bool grid_barrier_n(const GridBar& b, unsigned nblocks, long long limit) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned target = (barrier_epoch() += 1) * gridDim.x;
+    const unsigned target = (barrier_epoch() += 1) * nblocks;
     __threadfence();  // the block's writes before its arrival
     atomicAdd(b.count, 1u);
     volatile unsigned* vcount = b.count;
     int ok = 1;
     long long spins = 0;
     while ((int)(*vcount - target) < 0) {
-      if (++spins > kBarrierSpinLimit) {
+      if (++spins > limit) {
         ok = 0;
         break;
       }
@@ -69,6 +70,19 @@ __device__ __forceinline__ bool grid_barrier(const GridBar& b) {
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+__device__ __forceinline__ bool grid_barrier(const GridBar& b) {
+  return grid_barrier_n(b, gridDim.x, kBarrierSpinLimit);
+}
+
+// The barrier's failure path, for tests: one barrier that also waits for
+// `phantom` blocks that do not exist gives up after `limit` polls; status[0]
+// = TG_OK if it was passed, TG_E_TIMEOUT if it gave up.
+__global__ void k_barrier_check(GridBar b, unsigned phantom, long long limit, int* status) {
+  if (threadIdx.x == 0) barrier_epoch() = 0;
+  const bool ok = grid_barrier_n(b, gridDim.x + phantom, limit);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *status = ok ? TG_OK : TG_E_TIMEOUT;
 }
 
 // Grid total of the threads' partials v (added in their own precision within
@@ -425,6 +439,19 @@ cudaError_t pcg64(cudaStream_t s, bool mu0, Pcg64Args a) {
   }
   if (unit) return pcg_launch(a.g, k_pcg64<512, false, true>, k_pcg64<256, false, true>, s, a);
   return pcg_launch(a.g, k_pcg64<512, false, false>, k_pcg64<256, false, false>, s, a);
+}
+
+cudaError_t barrier_check(cudaStream_t s, unsigned* count, unsigned phantom, long long limit, int* status) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(4);
+  cfg.blockDim = dim3(64);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_barrier_check, GridBar{count}, phantom, limit, status);
 }
 
 cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a) {

@@ -110,6 +110,7 @@ SIGNATURES = {
     "tg_checkpoint_size": (C.c_size_t, [_vp]),
     "tg_checkpoint_save": (C.c_int, [_vp, _vp, C.c_size_t]),
     "tg_checkpoint_load": (C.c_int, [_vp, _vp, C.c_size_t]),
+    "tg_grid_barrier_check": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "tg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
     "tg_stage_faults": (C.c_int, [C.c_int, C.POINTER(C.c_uint)]),
     "tg_fm_propagator": (C.c_int, [_vp, C.POINTER(CgParams), C.POINTER(C.c_int), _dp, C.POINTER(CgResult)]),
