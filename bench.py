@@ -41,6 +41,7 @@ import numpy as np  # noqa: E402
 
 W = dict(nt=1024, nx=1024, m=0.05, g=0.6, mu=0.0, bc_t=-1, bc_x=1, sigma=0.3, nsteps=20, tau=1.0, rel_tol=1e-10,
          npf=1, seed=20241203)
+METRIC = "HMC trajectories/s (1024^2 plain FP64) + Dslash HBM GB/s"
 WORKLOAD_NAME = "1024x1024 plain-FP64 HMC trajectory (20 leapfrog steps, tau 1, CG rel 1e-10, m 0.05, g 0.6)"
 # Algorithmic bytes per site: one FP64 CG iteration (M^dag M 64 + x,r update 96 + p update 48)
 CG_ITER_BYTES_PER_SITE = 208
@@ -256,7 +257,7 @@ def run_reference(args, ws, rank):
         if i >= args.warmup:
             vals.append(cs["value"])
     v = statistics.median(vals)
-    line = {"impl": "reference", "metric": "HMC trajectories/s (1024^2 plain FP64)", "value": v,
+    line = {"impl": "reference", "metric": METRIC, "value": v,
             "unit": "trajectories/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "config": config_block(),
@@ -392,7 +393,7 @@ def run_ours(args, ws, rank, local):
     if rank != 0:
         return
     line = {
-        "metric": "HMC trajectories/s (1024^2 plain FP64) + Dslash HBM GB/s",
+        "metric": METRIC,
         "value": value, "unit": "trajectories/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded Gaussian A_mu, Philox pseudofermion/momentum fields)",
