@@ -376,9 +376,12 @@ def run_ours(args, ws, rank, local):
     hbm, peak_kind = peaks()
     t_iter_ms = cg_ms / max(1, iters)
     achieved = CG_ITER_BYTES_PER_SITE * V / (t_iter_ms * 1e-3) / 1e9
-    # one cooperative kernel per CG solve (the default, persistent solver), four
-    # kernels per MD step, about 20 for the heatbath and the sums
-    launches = sum(r.cg_solves for r in res) + args.steps * (4 * W["nsteps"] + 20)
+    # per trajectory (ncu launch list, profiles/hmc_trajectory_1024_fp64_launch_list.md):
+    # one cooperative kernel per CG solve (the default, persistent solver);
+    # nsteps + 1 gauge steps; per MD step the force's M chi and the momentum
+    # update; 17 for the heatbath, phi = M^dag eta, the action sums, the
+    # decision and the link phases
+    launches = sum(r.cg_solves for r in res) + args.steps * (3 * W["nsteps"] + 1 + 17)
 
     fp64_achieved = CG_ITER_FP64_FLOPS_PER_SITE * V / (t_iter_ms * 1e-3) / 1e12
     try:
