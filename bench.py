@@ -10,7 +10,7 @@ Workload (one "step" = one HMC trajectory of the hot path):
 
 Output: one JSON line (rank 0).  `value` is device-timed trajectories/s with the
 gauge field resident in HBM; `e2e` the same through the public C ABI with the
-gauge field uploaded from and downloaded to host memory every trajectory.
+gauge field uploaded from and downloaded to pinned host memory every trajectory.
 `roofline` is the CG iteration (inside k_pcg64, the persistent FP64 solver:
 one cooperative launch per solve, >99% of the device time), timed with CUDA
 events around the solves inside the trajectory graph, against the algorithmic
@@ -329,15 +329,16 @@ def run_ours(args, ws, rank, local):
     for r in res:
         assert r.status == 0, r.as_dict()
 
-    # ---- e2e through the public API with host buffers ----
-    A_host = L64.get_gauge()
+    # ---- e2e through the public API with pinned host buffers ----
+    A_host = torch.empty((nt, nx, 2), dtype=torch.float64, pin_memory=True).numpy()
+    L64.get_gauge(A_host)
     torch.cuda.synchronize()
     barrier(ws)
     t0 = time.perf_counter()
     for i in range(args.steps):
         L64.set_gauge(A_host)                    # H2D: 16 B/site
         r = L64.update_gauge(hp64)
-        A_host = L64.get_gauge()                 # D2H: 16 B/site + the result struct
+        L64.get_gauge(A_host)                    # D2H: 16 B/site + the result struct
     t_e2e = allmax(ws, time.perf_counter() - t0)
     e2e_value = ws * args.steps / t_e2e
 

@@ -81,10 +81,15 @@ class Lattice:
         A = _f64(A).reshape(self.nt, self.nx, 2)
         N.check(self.lib.tg_set_gauge(self.h, _p(A)))
 
-    def get_gauge(self) -> np.ndarray:
-        A = np.empty((self.nt, self.nx, 2))
-        N.check(self.lib.tg_get_gauge(self.h, _p(A)))
-        return A
+    def get_gauge(self, out: np.ndarray | None = None) -> np.ndarray:
+        """A as double[nt][nx][2]; into `out` (C-contiguous float64, for example a
+        pinned host buffer) when given."""
+        if out is None:
+            out = np.empty((self.nt, self.nx, 2))
+        elif out.dtype != np.float64 or not out.flags.c_contiguous or out.size != 2 * self.nt * self.nx:
+            raise ValueError("out must be a C-contiguous float64 array of nt * nx * 2 values")
+        N.check(self.lib.tg_get_gauge(self.h, _p(out)))
+        return out
 
     # -- checkpoint and resume ------------------------------------------------
     def checkpoint(self) -> bytes:
