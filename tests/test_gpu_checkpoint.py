@@ -75,6 +75,10 @@ def test_checkpoint_header_and_refusals(tg):
         L.restore(ck[:8] + struct.pack("<i", 2) + ck[12:])   # unknown version
     L.restore(ck)                                          # a good one still loads
     assert np.array_equal(L.get_gauge(), A)
+    out = np.full((8, 6, 2), np.nan)                       # into a caller's buffer
+    assert L.get_gauge(out) is out and np.array_equal(out, A)
+    with pytest.raises(ValueError):
+        L.get_gauge(np.empty((8, 6, 2), np.float32))
 
 
 BATCH = [dict(nt=16, nx=16, m=0.3, g=0.5, mu=0.0, bc_t=-1, bc_x=1, seed=71),
