@@ -10,6 +10,7 @@ the CUDA-event timings.  Numbers printed under a profiler are not benchmark
 values.
 
 Report modes:
+    --all-kernels                every kernel once, for a per-kernel ncu table
     --batch N [--sequential K]   N chains of mixed sizes in one batched launch
     --mixed-report --size 2048   FP64 vs mixed-precision solve and trajectories at m 0.02
     --scaling-report             dH against the leapfrog step at 64^2, two pseudofermions
@@ -44,7 +45,11 @@ def main():
     ap.add_argument("--mixed-report", action="store_true", help="the ill-conditioned (m 0.02) mixed-precision report")
     ap.add_argument("--mixed-tau", type=float, nargs="+", default=[1.0, 0.05],
                     help="trajectory lengths of the mixed-precision report")
+    ap.add_argument("--all-kernels", action="store_true",
+                    help="every kernel of the library once or a few times, for a per-kernel ncu table")
     a = ap.parse_args()
+    if a.all_kernels:
+        return all_kernels_case(a)
     if a.batch:
         return batch_case(a)
     if a.scaling_report:
@@ -71,6 +76,59 @@ def main():
         out["cg_iterations"] = res.iterations
         out["cg_status"] = N.STATUS_NAMES[res.status]
     L.close()
+    print(json.dumps(out))
+
+
+def all_kernels_case(a):
+    """Each kernel of the library at a size where its traffic leaves L2 where
+    that is possible: on 2048^2 (m 0.02, g 0.8, A ~ N(0, 0.5^2)) the operator
+    in both precisions, a short trajectory in each precision and scheduling
+    (CG to 1e-2 relative, 2 leapfrog steps, launched eagerly), the
+    measurements and the pure-gauge sweep; the fermion-bag operator, CG and
+    propagator, the dense matrix and the log-determinant on small lattices; one
+    trajectory of a 16-chain batch."""
+    import os
+
+    from .lattice import Batch, batch_params, hmc_params
+    os.environ["TG_GRAPH"] = "0"
+    out = {}
+    n = 2048
+    rng = np.random.default_rng(n)
+    L = Lattice(n, n, 0.02, 0.8, 0.0, N.BC_ANTIPERIODIC, N.BC_PERIODIC)
+    L.set_gauge(rng.normal(0, 0.5, (n, n, 2)))
+    out["ms_M64"] = L.time_apply(2, False, N.PREC_FP64)
+    out["ms_M32"] = L.time_apply(2, False, N.PREC_MIXED)
+    for prec in (N.PREC_FP64, N.PREC_MIXED):
+        for solver in (N.SOLVER_LAUNCHES, N.SOLVER_PERSISTENT):
+            hp = hmc_params(nsteps=2, tau=0.1, rng=N.RNG_PHILOX, seed=5, use_graph=False,
+                            cg=cg_params(rel_tol=1e-2, abs_tol2=0.0, precision=prec, ru_interval=50, solver=solver))
+            r = L.update_gauge(hp)
+            out[f"traj_p{prec}_s{solver}_its"] = r.cg_iterations
+    out["magnetisation"] = L.magnetisation()
+    out["pbp"] = L.chiral_condensate(2, seed=1, cp=cg_params(rel_tol=1e-4, abs_tol2=0.0))[0]
+    L.update_puregauge_hb(1)
+    L.close()
+    s = 64
+    L = Lattice(s, s, 0.3, 0.5, 0.0, N.BC_ANTIPERIODIC, N.BC_ANTIPERIODIC)
+    mask = (rng.random((s, s)) < 0.1).astype(np.int32)
+    v = rng.normal(size=(s, s))
+    L.fM(mask, v)
+    L.fM(mask, v, transpose=True)
+    out["cg_MdM_its"] = L.cg_MdM(mask, v)[1].iterations
+    L.close()
+    L = Lattice(8, 8, 0.3, 0.5, 0.0, N.BC_ANTIPERIODIC, N.BC_ANTIPERIODIC)
+    L.fm_propagator()
+    L.set_gauge(rng.normal(0, 0.3, (8, 8, 2)))
+    L.fermion_matrix()
+    out["log_det"] = L.log_det(rng.normal(0, 0.3, (64, 8, 8, 2)))[0][0]
+    L.close()
+    chains, fields = mixed_size_chains(16)
+    B = Batch(chains)
+    for i, A in enumerate(fields):
+        B.set_gauge(i, A)
+    B.trajectory(batch_params(nsteps=2, use_graph=False, block=451241,
+                              cg=cg_params(rel_tol=1e-6, abs_tol2=0.0, precision=N.PREC_MIXED)))
+    B.close()
     print(json.dumps(out))
 
 
