@@ -54,3 +54,51 @@ def test_reference_arm_runs_on_rank0_only(capsys):
         steps, warmup, gpus = 1, 0, 2
     bench.run_reference(Args(), ws=2, rank=1)   # rank 1: no work, no output
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_reports_the_whole_host(capsys, monkeypatch):
+    """Rank 0's reference line: one reference process per host core, `value` the
+    median over the timed steps of the host's summed trajectories/s, the serial
+    one-core figure beside it.  The samplers are replaced by fixed numbers."""
+    import multiprocessing
+    import statistics
+    sys.path.insert(0, ROOT)
+    import bench
+
+    class Pool:
+        def __init__(self, n):
+            self.n = n
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            return False
+
+    class Ctx:
+        pass
+    Ctx.Pool = Pool
+    seen = []
+
+    def host_sample(pool, cores, seconds, seed):
+        seen.append((pool.n, cores, seed))
+        return 0.004 + 0.001 * len(seen), "reference"
+    monkeypatch.setattr(multiprocessing, "get_context", lambda kind: Ctx)
+    monkeypatch.setattr(bench, "host_cores", lambda: 4)
+    monkeypatch.setattr(bench, "cpu_host_sample", host_sample)
+    monkeypatch.setattr(bench, "cpu_sample",
+                        lambda repeats=1: dict(value=0.001, kind="reference", cores=1, sample="one core"))
+
+    class Args:
+        steps, warmup, gpus = 3, 1, 1
+    bench.run_reference(Args(), ws=1, rank=0)
+    line = json.loads(capsys.readouterr().out.strip())
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC
+    assert len(seen) == 4 and all(n == 4 and c == 4 for n, c, _ in seen)
+    assert len({s for _, _, s in seen}) == 4                       # fresh fields every step
+    assert line["value"] == pytest.approx(statistics.median([0.006, 0.007, 0.008]))
+    cb = line["cpu_baseline"]
+    assert cb["cores"] == 4 and cb["value"] == line["value"] and cb["kind"] == "reference"
+    assert cb["single_process"] == {"value": 0.001, "cores": 1, "kind": "reference", "sample": "one core"}
+    assert line["e2e"] == {"value": line["value"], "unit": "trajectories/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
