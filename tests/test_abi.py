@@ -60,3 +60,23 @@ def test_compat_library_exports_reference_names(built):
 
 def test_hmc_program_built(built):
     assert os.access(built["hmc"], os.X_OK)
+
+
+def test_integration_example_compiles_as_c(built, tmp_path):
+    """The native-ABI example of INTEGRATION.md, wrapped in main(), compiles as
+    plain C99 against include/thirring_gpu.h and links against
+    libthirring_gpu.so (it is not run: no GPU here)."""
+    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
+        doc = f.read()
+    m = re.search(r"```c\n(#include \"thirring_gpu.h\"\n.*?)```", doc, flags=re.S)
+    assert m, "native-ABI example not found"
+    include, body = m.group(1).split("\n", 1)
+    src = tmp_path / "example.c"
+    src.write_text("#include <stdio.h>\n#include <stdlib.h>\n" + include + "\n"
+                   "static double A[1024 * 1024 * 2];\n"
+                   "int main(void) {\n" + body + "  return rc == TG_OK ? 0 : 1;\n}\n")
+    lib_dir = os.path.dirname(built["libthirring_gpu"])
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", f"-I{os.path.join(ROOT, 'include')}",
+                        str(src), "-o", str(tmp_path / "example"), f"-L{lib_dir}", "-lthirring_gpu",
+                        f"-Wl,-rpath,{lib_dir}"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
