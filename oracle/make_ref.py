@@ -35,7 +35,8 @@ mersenne_inline.c / mersenne.h are copied unchanged.  oracle/ref_driver.c (own
 code) #includes the generated file and exposes flat-array entry points; one
 shared library is built per (NT, NX, variant) into oracle/_ref/.
 
-/root/reference is read only here, at generation time.  The generated sources
+The reference tree (THIRRING2D_REF, default /root/reference) is read only
+here, at generation time.  The generated sources
 stay in oracle/_ref/src (git-ignored); where the reference tree is absent (the
 GPU host) the libraries are rebuilt from those generated sources if present.
 """
@@ -48,7 +49,8 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+# the reference checkout; THIRRING2D_REF overrides the default location
+REF_ROOT = os.environ.get("THIRRING2D_REF", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")
 

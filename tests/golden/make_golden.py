@@ -37,6 +37,11 @@ CONFIGS = {
     "mu_8x8_px": (8, 8, 0.3, 0.8, 0.3, "fixed_px", 0.3, 777, 5, 3, 10),
     # odd shape, mu on, reference BCs
     "odd_6x4_apx": (6, 4, 0.5, 1.0, 0.2, "fixed_apx", 0.5, 99, 5, 3, 8),
+    # column-march shapes (nx a multiple of 32, nt of 4), stable step sizes (|dH| < 1):
+    # the stencil path of the large-lattice workloads, against the reference
+    "march_64x64_px": (64, 64, 0.1, 0.5, 0.0, "fixed_px", 0.3, 6464, 10, 3, 80),
+    "march_32x96_apx": (32, 96, 0.2, 0.5, 0.0, "fixed_apx", 0.3, 3296, 10, 3, 40),
+    "march_32x64_mu_px": (32, 64, 0.2, 0.6, 0.2, "fixed_px", 0.3, 3264, 10, 3, 40),
 }
 
 MT_SEEDS = [12345, 4354365264, -7]
@@ -166,11 +171,14 @@ def make_prop():
 
 
 if __name__ == "__main__":
-    make_ref.build([(c[0], c[1]) for c in CONFIGS.values()] + [(4, 4), (6, 4)])
-    make_vecops()
-    make_free_det()
-    make_prop()
-    make_mt()
-    make_dense()
-    for name, cfg in CONFIGS.items():
-        make_config(name, *cfg)
+    # no arguments: every fixture; else only the named trajectory configs
+    names = sys.argv[1:] or list(CONFIGS)
+    make_ref.build(sorted({(CONFIGS[n][0], CONFIGS[n][1]) for n in names} | {(4, 4), (6, 4)}))
+    if not sys.argv[1:]:
+        make_vecops()
+        make_free_det()
+        make_prop()
+        make_mt()
+        make_dense()
+    for name in names:
+        make_config(name, *CONFIGS[name])

@@ -6,8 +6,11 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-TRAJ_CONFIGS = ["c1_16x16_apx", "c1_16x16_px", "c1s_16x16_px", "mu_8x8_px", "odd_6x4_apx"]
-STABLE = {"c1s_16x16_px", "mu_8x8_px", "odd_6x4_apx"}
+# trajectory fixtures whose nx is a multiple of 32 and nt of 4: they run the
+# column-march stencil, the path of the large-lattice workloads
+MARCH_CONFIGS = ["march_64x64_px", "march_32x96_apx", "march_32x64_mu_px"]
+TRAJ_CONFIGS = ["c1_16x16_apx", "c1_16x16_px", "c1s_16x16_px", "mu_8x8_px", "odd_6x4_apx"] + MARCH_CONFIGS
+STABLE = {"c1s_16x16_px", "mu_8x8_px", "odd_6x4_apx"} | set(MARCH_CONFIGS)
 
 
 def golden(name: str) -> dict:

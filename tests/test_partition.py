@@ -109,7 +109,8 @@ def audit(nt, nx, segments):
 # the persistent solver (152 x 512 or 304 x 256 threads); lattices whose nx is a
 # multiple of 32 use the march
 GRID_SHAPES = [(1, 8), (4, 16), (152, 16), (304, 8), (456, 8), (7, 8)]
-SHAPES = [(32, 32), (16, 32), (36, 32), (64, 96), (8, 64), (128, 128), (96, 128), (1024, 64), (4, 32), (2, 64)]
+SHAPES = [(32, 32), (16, 32), (36, 32), (64, 96), (8, 64), (128, 128), (96, 128), (1024, 64), (4, 32), (2, 64),
+          (64, 64), (32, 96), (32, 64)]
 
 
 @pytest.mark.parametrize("nt,nx", SHAPES)
