@@ -289,10 +289,13 @@ int tg_cg_mdm_masked(tg_lattice* L, const tg_cg_params* cp, const int* mask, con
  * lattices of at most 16384 sites (128 x 128); larger lattices get TG_E_ARG.
  * A_dev: gauge field double[nt*nx*2]; b_dev, x_dev: double2[nt*nx] on that
  * device; p->device is not used; stream may be NULL (the default stream).
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  All calls share the array and it
- * keeps the previous call's contents, so calls that overlap on the GPU race:
- * order them (one stream, or synchronize between them). */
+ * The first call on a device looks up the array's device address.  No call
+ * can run inside a stream capture: the solve reads its state back to the host
+ * and synchronizes the stream every 16 iterations, so a call on a capturing
+ * stream (or on the legacy default stream while another stream captures)
+ * returns TG_E_ARG before it enqueues anything.  All calls share the array
+ * and it keeps the previous call's contents, so calls that overlap on the GPU
+ * race: order them (one stream, or synchronize between them). */
 int tg_cg_noalloc(const tg_lattice_params* p, const tg_cg_params* cp, const void* A_dev, const void* b_dev,
                   void* x_dev, tg_cg_result* res, void* stream);
 

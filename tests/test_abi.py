@@ -80,3 +80,34 @@ def test_integration_example_compiles_as_c(built, tmp_path):
                         str(src), "-o", str(tmp_path / "example"), f"-L{lib_dir}", "-lthirring_gpu",
                         f"-Wl,-rpath,{lib_dir}"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     assert r.returncode == 0, r.stdout
+
+
+def test_noalloc_path_calls_no_allocator():
+    """tg_cg_noalloc (csrc/tg_noalloc.cu) and the explicit-grid launchers it
+    calls (the *_fixed functions and resident_grid_nocache of tg_kernels.cu)
+    name no allocating routine: no cudaMalloc* / cudaFree*, no cudaHostAlloc,
+    no library allocator (dmalloc), no torch."""
+    csrc = os.path.join(ROOT, "thirring2d_gb300", "csrc")
+
+    def code(text):
+        return re.sub(r"//[^\n]*", "", re.sub(r"/\*.*?\*/", "", text, flags=re.S))
+
+    with open(os.path.join(csrc, "tg_noalloc.cu")) as f:
+        bodies = [code(f.read())]
+    with open(os.path.join(csrc, "tg_kernels.cu")) as f:
+        kern = code(f.read())
+    for name in ("resident_grid_nocache", "link_phase_fixed", "cg64_init_fixed", "cg64_iter_fixed"):
+        m = re.search(r"\n[^\n]*\b" + name + r"\([^;{]*\)\s*\{", kern)
+        assert m, name
+        depth, i = 0, m.end() - 1
+        while True:  # the function body, by brace matching
+            depth += {"{": 1, "}": -1}.get(kern[i], 0)
+            i += 1
+            if depth == 0:
+                break
+        bodies.append(kern[m.start():i])
+    banned = re.compile(r"\b(cudaMalloc\w*|cudaFree\w*|cudaHostAlloc|cudaMallocHost|cuMem\w*Alloc\w*|dmalloc|"
+                        r"malloc|calloc|realloc|new\s|torch)\b")
+    for body in bodies:
+        hits = banned.findall(body)
+        assert not hits, hits

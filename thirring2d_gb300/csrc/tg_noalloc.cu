@@ -81,10 +81,24 @@ extern "C" int tg_cg_noalloc(const tg_lattice_params* p, const tg_cg_params* cp,
   if (cp->precision != TG_PREC_FP64) return record_error(TG_E_ARG, "tg_cg_noalloc: only the FP64 solver");
   if (cp->maxiter <= 0 || !(cp->rel_tol >= 0) || !(cp->abs_tol2 >= 0))
     return record_error(TG_E_ARG, "tg_cg_noalloc: bad CG parameters");
+  cudaStream_t s = (cudaStream_t)stream;
+  // An error left by an earlier, unrelated runtime call on this thread would
+  // otherwise surface at this function's first launch check: clear it here.
+  (void)cudaGetLastError();
+  // The solve copies its state to the host and synchronizes the stream every
+  // few iterations, which a stream under capture cannot do (and the sync
+  // would invalidate the caller's capture): refuse before enqueueing anything.
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t ce = cudaStreamIsCapturing(s, &cs);
+  if (ce != cudaSuccess) {
+    (void)cudaGetLastError();
+    return record_error(TG_E_ARG, "tg_cg_noalloc: cannot run while a stream capture is in progress");
+  }
+  if (cs != cudaStreamCaptureStatusNone)
+    return record_error(TG_E_ARG, "tg_cg_noalloc: cannot run on a stream that is being captured");
   unsigned char* base = nullptr;
   int rc = scratch_base(&base);
   if (rc != TG_OK) return rc;
-  cudaStream_t s = (cudaStream_t)stream;
 
   Geo g{};
   g.nt = p->nt;
