@@ -20,9 +20,13 @@ with the mixed-precision solver (FP32 CG + FP64 reliable updates every 50
 iterations) started from the same field and random stream.
 
 `--impl reference` times the reference hmc.c (adjoint-corrected build in
-oracle/_ref, single-threaded as the reference is) on a bounded sample: 20
-iterations of its fmdm_invert_cg at 1024^2 per step, scaled to a trajectory
-by the CG iteration count of the workload.
+oracle/_ref, serial as the reference is, one process per host core) on a
+bounded sample: its fmdm_invert_cg at 1024^2, 20 iterations per call, scaled to
+a trajectory by the workload's CG iterations, which that arm counts on the host
+(the reference's CG, restated in the oracle, to 1e-10 on the workload's first
+solve, times the solves of a trajectory).  A whole 1024^2 trajectory of the
+reference takes about 15 minutes of one core; on the 16^2 workload (`c1`) the
+reference's own update_gauge is timed whole, with no scaling.
 """
 from __future__ import annotations
 
@@ -46,10 +50,8 @@ WORKLOAD_NAME = "1024x1024 plain-FP64 HMC trajectory (20 leapfrog steps, tau 1, 
 # Algorithmic bytes per site: one FP64 CG iteration (M^dag M 64 + x,r update 96 + p update 48)
 CG_ITER_BYTES_PER_SITE = 208
 DSLASH_BYTES_PER_SITE = 64
-# CG iterations per trajectory of this workload (FP64 solver; sum over the 21
-# solves), measured by the GPU arm on GB300 and used to scale the reference's
-# per-iteration CPU time to a trajectory.
-CG_ITERS_PER_TRAJ = 7900
+# CG solves per trajectory: one per MD step (the force) and one for the final action
+SOLVES_PER_TRAJ = W["nsteps"] + 1
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -63,8 +65,8 @@ def peaks():
 
 
 # DRAM bytes (read + write) of one FP64 CG iteration of the persistent solver
-# (k_pcg64, 100 iterations in one launch) at 1024^2 from one ncu capture:
-# profiles/cg_iteration_1024_fp64_persistent.md.
+# (k_pcg64, 100 iterations in one launch) at 1024^2, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum over the launch / 100).
 CG_ITER_DRAM_BYTES = 116.4e6
 # FP64 work of one CG iteration per site, in flops (FMA = 2): two operator
 # applies (16 FMA + 2 MUL each), p' = r + beta p, x/r updates, two norms.
@@ -157,10 +159,11 @@ def replica_seed(rank: int) -> int:
 # ---------------------------------------------------------------------------
 # CPU reference timing (bounded sample)
 # ---------------------------------------------------------------------------
-def cpu_sample(repeats: int = 3):
+def cpu_sample(iters_per_traj: float, repeats: int = 3):
     """Seconds per CG iteration and per operator apply of the reference hmc.c at
     1024^2 (oracle/_ref sample build: fmdm_invert_cg stops after 20 iterations),
-    or of the oracle restatement where the reference build is absent."""
+    or of the oracle restatement where the reference build is absent, scaled
+    to a trajectory of `iters_per_traj` CG iterations."""
     from oracle import oracle as O
     rng = np.random.default_rng(W["seed"])
     A = rng.normal(0, W["sigma"], (W["nt"], W["nx"], 2))
@@ -192,10 +195,11 @@ def cpu_sample(repeats: int = 3):
     t_iter = min(ts) / iters
     # per trajectory: CG iterations + the non-CG applies (phi = M^dag eta, M chi per
     # MD step, two stochastic-term applies)
-    t_traj = t_iter * CG_ITERS_PER_TRAJ + t_apply * (W["nsteps"] + 3)
+    t_traj = t_iter * iters_per_traj + t_apply * (W["nsteps"] + 3)
     sample = (f"{repeats} x {iters} iterations of fmdm_invert_cg + 1 fm_mul at {W['nt']}x{W['nx']} "
               f"({'reference hmc.c build' if kind == 'reference' else 'oracle restatement'}), "
-              f"scaled by {CG_ITERS_PER_TRAJ} CG iterations and {W['nsteps'] + 3} applies per trajectory")
+              f"scaled by {iters_per_traj:.0f} CG iterations (counted by the GPU arm of this run) and "
+              f"{W['nsteps'] + 3} applies per trajectory")
     return dict(value=1.0 / t_traj, unit="trajectories/s", cores=1, kind=kind, sample=sample,
                 sec_per_cg_iter=t_iter, sec_per_apply=t_apply)
 
@@ -229,7 +233,7 @@ def _ref_traj_rate(job):
     reference's own fmdm_invert_cg (oracle/_ref sample build: 20 iterations per
     call) timed for about `seconds` and one fm_mul, scaled like cpu_sample; the
     oracle restatement where that build is absent.  Runs in its own process."""
-    seconds, seed = job
+    seconds, seed, iters_per_traj = job
     from oracle import oracle as O
     rng = np.random.default_rng(seed)
     A = rng.normal(0, W["sigma"], (W["nt"], W["nx"], 2))
@@ -249,19 +253,33 @@ def _ref_traj_rate(job):
         step()
         n += 1
     t_iter = (time.perf_counter() - t0) / (20 * n)
-    return 1.0 / (t_iter * CG_ITERS_PER_TRAJ + t_apply * (W["nsteps"] + 3)), kind
+    return 1.0 / (t_iter * iters_per_traj + t_apply * (W["nsteps"] + 3)), kind
 
 
 def host_cores() -> int:
     return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
 
 
-def cpu_host_sample(pool, cores: int, seconds: float, seed: int):
+def cpu_host_sample(pool, cores: int, seconds: float, seed: int, iters_per_traj: float):
     """The 1024^2 workload on the whole host: the reference is serial, so every
     core runs its own reference process (an independent chain) at the same time;
     the host's trajectories/s is the sum over the processes."""
-    out = pool.map(_ref_traj_rate, [(seconds, seed + k) for k in range(cores)])
+    out = pool.map(_ref_traj_rate, [(seconds, seed + k, iters_per_traj) for k in range(cores)])
     return sum(r for r, _ in out), out[0][1]
+
+
+def host_iteration_count():
+    """CG iterations of the workload's first solve, counted on the host with the
+    reference's CG (fmdm_invert_cg, hmc.c:341-404, restated in the oracle and
+    bitwise equal to it) stopped at the workload's 1e-10 relative residual:
+    phi = M^dag eta on the starting field, as random_pseudofermion draws it."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(W["seed"])
+    A = rng.normal(0, W["sigma"], (W["nt"], W["nx"], 2))
+    eta = rng.normal(size=(W["nt"], W["nx"])) + 1j * rng.normal(size=(W["nt"], W["nx"]))
+    o = O.Oracle(W["nt"], W["nx"], W["m"], W["g"], W["mu"], W["bc_t"], W["bc_x"])
+    _, st, it = o.cg(A, o.Mdag(A, eta), rel_tol=W["rel_tol"], abs_tol2=0.0)
+    return it
 
 
 def cpu_batch_sample(chains, iterations, seconds: float = 4.0):
@@ -287,25 +305,82 @@ def cpu_batch_sample(chains, iterations, seconds: float = 4.0):
                       f"trajectory plus 13 applies"}
 
 
+def _quiet_stdout():
+    """Pool initializer: the reference's update_gauge prints its action lines
+    and decision (hmc.c:701, 735-743); send the worker's stdout to /dev/null."""
+    fd = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(fd, 1)
+
+
+def _ref_c1_rate(job):
+    """Whole trajectories/s of the 16^2 workload on one host core: the
+    reference's own update_gauge (hmc.c:671-746, 10 steps, its CG stop
+    |r|^2 < 1e-30) on its own chain, after one untimed trajectory; the oracle
+    restatement's trajectory where the reference build is absent."""
+    seconds, k = job
+    from oracle import oracle as O
+    from thirring2d_gb300.workloads import C1, c1_chains
+    _, fields = c1_chains(k + 1, seed=160)
+    A = np.ascontiguousarray(fields[k])
+    nt, nx = C1["nt"], C1["nx"]
+    if O.ref_available(nt, nx, "fixed_px"):
+        ref = O.RefHMC(nt, nx, C1["m"], C1["g"], C1["mu"], seed=1000 + k, warmup=543210, variant="fixed_px")
+        ref.set_A(A)
+        kind, step = "reference", ref.update_gauge
+    else:
+        o = O.Oracle(nt, nx, C1["m"], C1["g"], C1["mu"], C1["bc_t"], C1["bc_x"])
+        mt = O.MT(1000 + k, 543210)
+        kind, step = "port", (lambda: o.trajectory(A, mt, C1["nsteps"], C1["tau"], 1, True))
+    step()
+    n, t0 = 0, time.perf_counter()
+    while n == 0 or time.perf_counter() - t0 < seconds:
+        step()
+        n += 1
+    return n / (time.perf_counter() - t0), n, kind
+
+
+def cpu_c1(seconds: float = 3.0):
+    """The 16^2 workload on the host, timed whole: one reference process on one
+    core, then one per host core at the same time (independent chains)."""
+    import multiprocessing as mp
+    cores = host_cores()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(1, initializer=_quiet_stdout) as pool:
+        one, n1, kind = pool.map(_ref_c1_rate, [(seconds, 0)])[0]
+    with ctx.Pool(cores, initializer=_quiet_stdout) as pool:
+        out = pool.map(_ref_c1_rate, [(seconds, k) for k in range(cores)])
+    return {"value": sum(r for r, _, _ in out), "unit": "trajectories/s", "cores": cores, "kind": kind,
+            "trajectories_timed": sum(n for _, n, _ in out),
+            "single_process": {"value": one, "cores": 1, "trajectories_timed": n1},
+            "sample": f"whole trajectories of the reference's own update_gauge (hmc.c:671-746; 10 steps, CG to "
+                      f"|r|^2 < 1e-30), one process per core ({cores}), each on its own chain for {seconds:.0f} s; "
+                      f"value = the sum over the processes; no scaling"}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
     import multiprocessing as mp
+    # the trajectory's CG iterations, counted on the host: the first solve of the
+    # workload times the solves of a trajectory
+    first_solve = host_iteration_count()
+    iters_per_traj = first_solve * SOLVES_PER_TRAJ
     # the serial reference as it runs, one process on one core (for context)
-    single = cpu_sample(repeats=1)
+    single = cpu_sample(iters_per_traj, repeats=1)
     # the whole host: one reference process per core, all at once; each step is
     # one such sample of `seconds` per process
     cores, seconds = host_cores(), 5.0
     vals = []
     with mp.get_context("spawn").Pool(cores) as pool:
         for i in range(args.warmup + args.steps):
-            v, kind = cpu_host_sample(pool, cores, seconds, 7000 + 100 * i)
+            v, kind = cpu_host_sample(pool, cores, seconds, 7000 + 100 * i, iters_per_traj)
             if i >= args.warmup:
                 vals.append(v)
     v = statistics.median(vals)
     sample = (f"{cores} concurrent reference processes (one per host core, independent chains), each timing "
               f"{seconds:.0f} s of fmdm_invert_cg (20 iterations per call) and one fm_mul at {W['nt']}x{W['nx']}, "
-              f"scaled by {CG_ITERS_PER_TRAJ} CG iterations and {W['nsteps'] + 3} applies per trajectory; "
+              f"scaled by {iters_per_traj} CG iterations ({first_solve} counted on the host for the workload's "
+              f"first solve, times {SOLVES_PER_TRAJ} solves) and {W['nsteps'] + 3} applies per trajectory; "
               f"value = the sum over the processes")
     line = {"impl": "reference", "metric": METRIC, "value": v,
             "unit": "trajectories/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -314,7 +389,11 @@ def run_reference(args, ws, rank):
             "cpu_baseline": {"value": v, "unit": "trajectories/s", "cores": cores, "kind": kind, "sample": sample,
                              "single_process": {"value": single["value"], "cores": 1, "kind": single["kind"],
                                                 "sample": single["sample"]}},
-            "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cg_iterations": {"first_solve_counted_on_host": first_solve, "per_traj_used": iters_per_traj,
+                              "note": "the GPU arm counts every solve of its trajectories (cg_iterations_per_traj "
+                                      "of its line); later solves of the MD run longer than the first, so this "
+                                      "count makes the reference's trajectory shorter than it is"}}
     print(json.dumps(line))
 
 
@@ -425,11 +504,13 @@ def run_ours(args, ws, rank, local):
     mixed_value = ws * args.steps / (ms_mx / 1000.0)
 
     batched = run_batched(tg, torch, dev, args) if not args.no_batched else None
+    stable = run_stable(tg, torch, dev, A0, replica_seed(rank), flush) if ws == 1 else None
+    c1 = run_c1(tg, torch, dev) if (ws == 1 and not args.no_c1) else None
 
     hbm, peak_kind = peaks()
     t_iter_ms = cg_ms / max(1, iters)
     achieved = CG_ITER_BYTES_PER_SITE * V / (t_iter_ms * 1e-3) / 1e9
-    # per trajectory (ncu launch list, profiles/hmc_trajectory_1024_fp64_launch_list.md):
+    # per trajectory (from an ncu launch list of this workload):
     # one cooperative kernel per CG solve (the default, persistent solver);
     # nsteps + 1 gauge steps; per MD step the force's M chi and the momentum
     # update; 17 for the heatbath, phi = M^dag eta, the action sums, the
@@ -461,7 +542,7 @@ def run_ours(args, ws, rank, local):
                      "peak_source": peak_kind, "bytes_per_site": CG_ITER_BYTES_PER_SITE,
                      "ms_per_iteration": t_iter_ms,
                      "traffic": CG_ITER_DRAM_BYTES,
-                     "traffic_source": "profiles/cg_iteration_1024_fp64_persistent.md (ncu, one capture)",
+                     "traffic_source": "ncu, one capture of k_pcg64 at 1024^2, DRAM read + write per iteration",
                      "note": "the FP64 CG is bound by the FP64 pipe, not HBM: at 88 flops per 208 B "
                              "and the measured FP64 rate, the pipe caps this HBM fraction at "
                              f"{fp64_peak_for_cap(hbm):.2f}; fp64_alu.frac is the fraction of the measured "
@@ -478,14 +559,115 @@ def run_ours(args, ws, rank, local):
                   "reliable_updates_per_traj": statistics.mean(r.reliable_updates for r in res_mx),
                   "dH_pairs_fp64_vs_mixed": mx_pairs},
         "batched": batched,
+        "stable": stable,
+        "c1": c1,
         "cg_iterations_per_traj": iters / args.steps,
         "dH": [r.dH for r in res], "accepted": [r.accepted for r in res],
         "clocks": clocks, "gpu_launches": launches,
     }
     if ws == 1:
-        cs = cpu_sample()
+        cs = cpu_sample(iters / args.steps)
         line["cpu_baseline"] = {k: cs[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))
+
+
+STABLE_TAU = 0.05
+
+
+def run_stable(tg, torch, dev, A0, seed, flush, ntraj=4):
+    """The 1024^2 lattice and starting field of the headline at a stable
+    trajectory length (tau 0.05, 20 steps: |dH| ~ 1), FP64 and mixed on the same
+    Philox stream: trajectories/s (CUDA events, the first trajectory of each run
+    untimed), dH of each, their difference and the accept decisions.  At the
+    workload's CG tolerance and at 1e-13, where the mixed dH matches FP64 to the
+    1e-9 target."""
+    nt, nx = W["nt"], W["nx"]
+    out = {"lattice": f"{nt}x{nx}", "tau": STABLE_TAU, "nsteps": W["nsteps"], "trajectories": ntraj,
+           "timed": ntraj - 1}
+    for tol in (W["rel_tol"], 1e-13):
+        runs = {}
+        for name, prec in (("fp64", tg.native.PREC_FP64), ("mixed", tg.native.PREC_MIXED)):
+            L = tg.Lattice(nt, nx, W["m"], W["g"], W["mu"], W["bc_t"], W["bc_x"], device=dev.index)
+            L.set_gauge(A0)
+            hp = tg.hmc_params(nsteps=W["nsteps"], tau=STABLE_TAU, npf=W["npf"], stochastic_term=True,
+                               rng=tg.native.RNG_PHILOX, seed=seed, use_graph=True,
+                               cg=tg.cg_params(rel_tol=tol, abs_tol2=0.0, precision=prec, ru_interval=50))
+            stream = torch.cuda.ExternalStream(L.lib.tg_stream(L.h), device=dev)
+            res, ms = [], 0.0
+            for k in range(ntraj):
+                with torch.cuda.stream(stream):
+                    flush.fill_(float(k))
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                r = L.update_gauge(hp)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                assert r.status == 0, r.as_dict()
+                if k > 0:
+                    ms += e0.elapsed_time(e1)
+                res.append(r)
+            L.close()
+            runs[name] = (res, (ntraj - 1) / (ms / 1e3))
+        (r64, v64), (rmx, vmx) = runs["fp64"], runs["mixed"]
+        out[f"cg_rel_{tol:g}"] = {
+            "fp64": v64, "mixed": vmx, "unit": "trajectories/s", "speedup_mixed_vs_fp64": vmx / v64,
+            "dH_fp64": [r.dH for r in r64], "dH_mixed": [r.dH for r in rmx],
+            "max_abs_dH_diff": max(abs(a.dH - b.dH) for a, b in zip(r64, rmx)),
+            "accepted_fp64": [r.accepted for r in r64], "accepted_mixed": [r.accepted for r in rmx],
+            "accept_agree": all(a.accepted == b.accepted for a, b in zip(r64, rmx)),
+            "cg_iterations_per_traj": {"fp64": statistics.mean(r.cg_iterations for r in r64),
+                                       "mixed": statistics.mean(r.cg_iterations for r in rmx)}}
+    return out
+
+
+def run_c1(tg, torch, dev, ntraj=200, nchains=512, batch_steps=5):
+    """The 16^2 plain-FP64 workload as the reference runs it (periodic x, m 0.1,
+    g 0.5, A ~ N(0, 0.1^2), 10 steps, tau 1): one chain on the FP64 path on the
+    reference's MT stream, with the reference's CG stop (|r|^2 < 1e-30) and with
+    the workload's 1e-12 relative stop, `ntraj` trajectories each through the C
+    ABI (wall clock, one host sync per trajectory); then `nchains` such chains in
+    one batch, FP64 and mixed at 1e-12; then the reference's own update_gauge,
+    timed whole on the host's cores."""
+    from thirring2d_gb300.workloads import C1, c1_chains
+    chains, fields = c1_chains(nchains)
+    out = {"config": "16x16, t antiperiodic, x periodic, m 0.1, g 0.5, mu 0, A ~ N(0, 0.1^2), 10 leapfrog steps, "
+                     "tau 1, one pseudofermion", "single_chain": {}}
+    for label, cp in (("fp64_cg_abs_1e-30", tg.cg_params()),
+                      ("fp64_cg_rel_1e-12", tg.cg_params(rel_tol=1e-12, abs_tol2=0.0))):
+        L = tg.Lattice(C1["nt"], C1["nx"], C1["m"], C1["g"], C1["mu"], C1["bc_t"], C1["bc_x"], device=dev.index)
+        L.set_gauge(fields[0])
+        L.seed_mersenne(1000, 543210)
+        hp = tg.hmc_params(nsteps=C1["nsteps"], tau=C1["tau"], rng=tg.native.RNG_MT, cg=cp)
+        for _ in range(3):
+            L.update_gauge(hp)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = [L.update_gauge(hp) for _ in range(ntraj)]
+        dt = time.perf_counter() - t0
+        L.close()
+        out["single_chain"][label] = {"value": ntraj / dt, "unit": "trajectories/s", "trajectories": ntraj,
+                                      "cg_iterations_per_traj": statistics.mean(r.cg_iterations for r in res),
+                                      "acceptance": statistics.mean(r.accepted for r in res)}
+    batch = {"chains": nchains}
+    for name, prec in (("fp64", tg.native.PREC_FP64), ("mixed", tg.native.PREC_MIXED)):
+        B = tg.Batch(chains)
+        for i, A in enumerate(fields):
+            B.set_gauge(i, A)
+        cg = tg.cg_params(rel_tol=1e-12, abs_tol2=0.0, precision=prec, ru_interval=50)
+        block, _ = B.autotune(tg.batch_params(nsteps=C1["nsteps"], cg=cg))
+        bp = tg.batch_params(nsteps=C1["nsteps"], cg=cg, block=block)
+        B.trajectory(bp)
+        ms = sum(B.trajectory(bp)[0].cg_ms for _ in range(batch_steps))
+        B.close()
+        batch[name] = {"value": nchains * batch_steps / (ms / 1e3), "unit": "chain-trajectories/s",
+                       "cg_rel_tol": 1e-12, "kernel_instance": block}
+    out["batch"] = batch
+    out["reference_host"] = cpu_c1()
+    ref = out["reference_host"]["value"]
+    out["speedup_vs_reference_host"] = {
+        "single_chain_fp64_same_cg_stop": out["single_chain"]["fp64_cg_abs_1e-30"]["value"] / ref,
+        "batch_fp64": batch["fp64"]["value"] / ref, "batch_mixed": batch["mixed"]["value"] / ref}
+    return out
 
 
 def run_batched(tg, torch, dev, args, nchains=512, sample=32):
@@ -495,7 +677,7 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
     single-lattice path (a sample of `sample` chains, scaled).  The same
     comparison is repeated at CG 1e-12, where the mixed batch matches the FP64
     batch's dH to 1e-9 on every chain whose MD is stable."""
-    from thirring2d_gb300.profile_case import mixed_size_chains
+    from thirring2d_gb300.workloads import mixed_size_chains
     chains, fields = mixed_size_chains(nchains)
     steps = max(1, args.steps)
 
@@ -527,15 +709,21 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
             L.close()
         return sample / (seq_ms / 1e3)
 
-    def compare(tol, block):
+    def compare(tol, block, block64):
         """First trajectory of the mixed and the FP64 batch from the same fields
-        and Philox stream, then `steps` timed mixed trajectories."""
+        and Philox stream, then `steps` timed trajectories of each (each batch on
+        its own autotuned kernel instance)."""
         Bm, bpm = make(cg(tg.native.PREC_MIXED, tol), block)
         if block == 0:
             block, _ = Bm.autotune(bpm)
             bpm = tg.batch_params(nsteps=10, cg=cg(tg.native.PREC_MIXED, tol), block=block)
-        B64, bp64 = make(cg(tg.native.PREC_FP64, tol), block)
+        B64, bp64 = make(cg(tg.native.PREC_FP64, tol), block64)
+        if block64 == 0:
+            block64, _ = B64.autotune(bp64)
+            bp64 = tg.batch_params(nsteps=10, cg=cg(tg.native.PREC_FP64, tol), block=block64)
         first_m, first_64 = Bm.trajectory(bpm), B64.trajectory(bp64)
+        ms64 = sum(B64.trajectory(bp64)[0].cg_ms for _ in range(steps))
+        rate64 = nchains * steps / (ms64 / 1e3)
         B64.close()
         # chains whose MD is stable at this step size (|dH| < 5): the absolute dH error there
         stable = [(a, b) for a, b in zip(first_m, first_64) if abs(b.dH) < 5.0]
@@ -547,11 +735,15 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
         Bm.close()
         rate = nchains * steps / (ms / 1e3)
         seq = sequential(cg(tg.native.PREC_FP64, tol))
-        return block, [r.cg_iterations for r in first_64], {
+        return block, block64, [r.cg_iterations for r in first_64], {
             "value": rate, "unit": "chain-trajectories/s", "cg_rel_tol": tol, "ms_per_batch_trajectory": ms / steps,
+            "fp64_batch": {"value": rate64, "unit": "chain-trajectories/s", "ms_per_batch_trajectory": ms64 / steps,
+                           "kernel_instance": block64},
             "sequential_fp64": {"value": seq, "unit": "chain-trajectories/s",
                                 "sample": f"{sample} of the {nchains} chains, one at a time, second trajectory each"},
             "speedup_vs_sequential_fp64": rate / seq,
+            "batching_factor_fp64": rate64 / seq,
+            "precision_factor_batch": rate / rate64,
             "dH_vs_fp64_batch": {
                 "stable_chains": len(stable),
                 "max_abs_err_stable_chains": max((abs(a.dH - b.dH) for a, b in stable), default=0.0),
@@ -561,8 +753,8 @@ def run_batched(tg, torch, dev, args, nchains=512, sample=32):
             "acceptance": float(np.mean([r.accepted for r in res[-1]])),
             "cg_iterations_per_chain_traj": float(np.mean([r.cg_iterations for r in res[-1]]))}
 
-    cfg, iters64, main = compare(1e-10, 0)
-    _, _, matched = compare(1e-12, cfg)
+    cfg, cfg64, iters64, main = compare(1e-10, 0, 0)
+    _, _, _, matched = compare(1e-12, cfg, cfg64)
     main["dH_vs_fp64_batch"]["note"] = ("chains with |dH| >= 5 have unstable MD at this step size, where dH differs "
                                         "chaotically between precisions; the decisions still agree")
     out = {"chains": nchains, "sites": int(sum(c["nt"] * c["nx"] for c in chains)),
@@ -579,6 +771,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-chain measurement")
+    ap.add_argument("--no-c1", action="store_true", help="skip the 16^2 workload leg")
     args = ap.parse_args()
     ws, rank, local = dist_init()
     if args.impl == "reference":

@@ -134,6 +134,12 @@ void ref_momentum_step(double* p, const double* psi, const double* st, double ep
 }
 void ref_gauge_step(const double* p, double eps) { mom_in(p); gauge_step(A, momv, eps); }
 
+/* The reference's own update_gauge (hmc.c:671-746: 10 leapfrog steps of a
+ * trajectory of length 1, its CG stopping at |r|^2 < 1e-30), called as the
+ * main loop of hmc.c:932-939 calls it.  It prints its action lines and the
+ * decision to stdout.  Used to time whole reference trajectories. */
+void ref_update_gauge(void) { update_gauge(A); }
+
 /* One trajectory with the sequence of update_gauge (hmc.c:671-746) built from
  * the reference's own functions, with nsteps/tau as arguments (the reference
  * hard-codes 10 and 1) and the stats returned at full precision instead of

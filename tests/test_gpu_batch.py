@@ -106,7 +106,7 @@ def test_cluster_instances_match_block_instance(tg, instance):
     """Chains split over thread-block clusters (2 or 4 blocks, distributed
     shared memory sums) against one block per chain: the same trajectories to
     the rounding of the team sums."""
-    from thirring2d_gb300.profile_case import mixed_size_chains
+    from thirring2d_gb300.workloads import mixed_size_chains
     chains, fields = mixed_size_chains(24, seed=9)
     runs = {}
     for inst in (51201, instance):
@@ -147,7 +147,7 @@ def test_batch_mixed_dH_within_1e9_at_tight_tolerance(tg):
     reproduces the FP64 batch's dH to 1e-9 on every chain whose MD is stable
     (|dH| < 5 at this step size), and makes the same accept/reject decisions on
     all chains."""
-    from thirring2d_gb300.profile_case import mixed_size_chains
+    from thirring2d_gb300.workloads import mixed_size_chains
     chains, fields = mixed_size_chains(128)
     out = []
     for precision in (0, 1):

@@ -24,6 +24,7 @@ import numpy as np
 
 from . import native as N
 from .lattice import Lattice, cg_params
+from .workloads import mixed_size_chains
 
 
 def main():
@@ -130,21 +131,6 @@ def all_kernels_case(a):
                               cg=cg_params(rel_tol=1e-6, abs_tol2=0.0, precision=N.PREC_MIXED)))
     B.close()
     print(json.dumps(out))
-
-
-def mixed_size_chains(n: int, seed: int = 4, side: int = 0):
-    """The batched-chain workload: n chains, sides uniform in {16, 24, 32, 48, 64,
-    96, 128} (or all `side`), m ~ U[0.05, 0.5], g ~ U[0.2, 1.2], own seeds,
-    A ~ N(0, 0.2^2)."""
-    rng = np.random.default_rng(seed)
-    sides = np.array([side] if side else [16, 24, 32, 48, 64, 96, 128])
-    chains, fields = [], []
-    for k in range(n):
-        L = int(rng.choice(sides))
-        chains.append(dict(nt=L, nx=L, m=float(rng.uniform(0.05, 0.5)), g=float(rng.uniform(0.2, 1.2)), mu=0.0,
-                           bc_t=N.BC_ANTIPERIODIC, bc_x=N.BC_PERIODIC, seed=int(seed * 100000 + k)))
-        fields.append(rng.normal(0, 0.2, (L, L, 2)))
-    return chains, fields
 
 
 def batch_case(a):
