@@ -73,6 +73,8 @@ double gauge_step(double*** A, double*** mom, double eps);                      
 double calc_gauge_action(double*** A);                                                   /* hmc.c:73  */
 void update_puregauge_hb(double*** A);                                                   /* hmc.c:82  */
 void update_gauge(double*** A);                                                          /* hmc.c:671 */
+void fermion_matrix(_Complex double* M);  /* hmc.c:269: M[i + j*V], global A; V <= 4096 */
+_Complex double determinant(void);        /* hmc.c:314: global A; V <= 1024; overflows as hmc.c's */
 double fermion_phase(double*** A);                                                       /* hmc.c:794 */
 void measure(void);                                                                      /* hmc.c:823 */
 

@@ -86,3 +86,73 @@ def test_hmc_program_jsonl_log(tmp_path):
     assert printed == [r["dH"] for r in rows]
     assert decisions == ["ACCEPTED" if r["accepted"] else "REJECTED" for r in rows]
     assert all(r["cg_solves"] == 11 and r["cg_iterations"] > 0 and r["cg_ms"] > 0 for r in rows)
+
+
+DENSE_PROGRAM = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include <complex.h>
+#include "thirring_hmc.h"
+/* argv: nt nx m mu A.bin out.bin -- A double[nt][nx][2]; out: M as hmc.c stores
+ * it (V*V complex, M[i + j*V]) then det M (re, im) */
+int main(int argc, char** argv) {
+  if (argc != 7) return 2;
+  int nt = atoi(argv[1]), nx = atoi(argv[2]);
+  m = atof(argv[3]);
+  mu = atof(argv[4]);
+  g = 0.5;
+  thirring_hmc_set_lattice(nt, nx);
+  FILE* f = fopen(argv[5], "rb");
+  if (!f) return 3;
+  A = malloc(nt * sizeof(double**));
+  for (int t = 0; t < nt; t++) {
+    A[t] = malloc((nx + 1) * sizeof(double*));
+    for (int x = 0; x < nx + 1; x++) {
+      A[t][x] = calloc(2, sizeof(double));
+      if (x < nx && fread(A[t][x], sizeof(double), 2, f) != 2) return 4;
+    }
+  }
+  fclose(f);
+  int V = nt * nx;
+  _Complex double* M = malloc((size_t)V * V * sizeof(_Complex double));
+  fermion_matrix(M);
+  _Complex double d = determinant();
+  double dd[2] = {creal(d), cimag(d)};
+  FILE* o = fopen(argv[6], "wb");
+  fwrite(M, sizeof(_Complex double), (size_t)V * V, o);
+  fwrite(dd, sizeof(double), 2, o);
+  fclose(o);
+  return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("name", ["det_4x4_apx", "det_4x4_px", "det_6x4_apx"])
+def test_compat_fermion_matrix_and_determinant(tmp_path, name):
+    """fermion_matrix(M) and determinant() of the reference-signature layer
+    (hmc.c:269-336, for the global A) against the reference's own dense matrix
+    and its log-determinant (tests/golden/det_*), called from plain C."""
+    from helpers import golden
+    d = golden(name)
+    nt, nx = int(d["nt"]), int(d["nx"])
+    src = tmp_path / "dense.c"
+    src.write_text(DENSE_PROGRAM)
+    lib_dir = os.path.join(ROOT, "thirring2d_gb300")
+    exe = tmp_path / "dense"
+    r = subprocess.run(["gcc", "-std=c99", "-O1", f"-I{os.path.join(ROOT, 'include')}", str(src), "-o", str(exe),
+                        f"-L{lib_dir}", "-lthirring_hmc", f"-Wl,-rpath,{lib_dir}", "-lm"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    np.ascontiguousarray(d["A"], dtype=np.float64).tofile(tmp_path / "A.bin")
+    env = dict(os.environ, HMC_BC_X="periodic" if int(d["bc_x"]) == 1 else "antiperiodic")
+    r = subprocess.run([str(exe), str(nt), str(nx), repr(float(d["m"])), repr(float(d["mu"])),
+                        str(tmp_path / "A.bin"), str(tmp_path / "out.bin")], capture_output=True, text=True,
+                       env=env, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = np.fromfile(tmp_path / "out.bin", dtype=np.float64)
+    V = nt * nx
+    M = (out[:2 * V * V:2] + 1j * out[1:2 * V * V:2]).reshape(V, V).T   # hmc.c's M[i + j*V]
+    assert np.abs(M - d["M"]).max() < 1e-14
+    det = out[2 * V * V] + 1j * out[2 * V * V + 1]
+    want = np.exp(float(d["logabsdet"])) * complex(d["phase"])
+    assert abs(det - want) <= 1e-10 * abs(want)

@@ -405,6 +405,38 @@ void update_gauge(double*** a) {
   }
 }
 
+/* hmc.c:269-310: the dense V x V matrix of fm_mul for the global A, stored as
+ * hmc.c stores it for LAPACK: element (row i, column j) at M[i + j*V].  The
+ * couplings are read at every call (hmc.c caches exp(+-mu) at the first). */
+void fermion_matrix(_Complex double* M) {
+  tg_lattice* L = ctx();
+  upload_gauge(A);
+  const size_t V = (size_t)NT_ * NX_;
+  double* Md = malloc(2 * V * V * sizeof(double));
+  if (!Md) {
+    fprintf(stderr, "thirring_hmc: fermion_matrix: out of host memory\n");
+    exit(1);
+  }
+  if (tg_dense_M(L, Md) != TG_OK) fatal("tg_dense_M");
+  for (size_t i = 0; i < V; i++)
+    for (size_t j = 0; j < V; j++) M[i + j * V] = Md[2 * (i * V + j)] + I * Md[2 * (i * V + j) + 1];
+  free(Md);
+}
+
+/* hmc.c:314-336: det M for the global A.  hmc.c multiplies the diagonal of a
+ * LAPACK LU; here the library's GPU LU gives log|det M| and arg det M, and the
+ * product is formed once.  As in hmc.c the value overflows a double (inf or
+ * NaN parts) once |det M| exceeds 1.8e308 on larger lattices; tg_log_det
+ * keeps the logarithm.  V <= 1024. */
+double complex determinant(void) {
+  tg_lattice* L = ctx();
+  upload_gauge(A);
+  double logabs = 0, phase = 0;
+  if (tg_log_det(L, 1, NULL, &logabs, &phase) != TG_OK) fatal("tg_log_det");
+  const double r = exp(logabs);
+  return r * cos(phase) + I * (r * sin(phase));
+}
+
 /* hmc.c:794-815: 20 stochastic sources, Im c^dag M^dag c averaged. */
 double fermion_phase(double*** a) {
   tg_lattice* L = ctx();
