@@ -137,23 +137,122 @@ VSRC = os.path.join(SRC, "vecops")
 VEC_SIZES = [(8, 8), (6, 4), (16, 16)]
 
 
+# declarations of the LAPACK routines the reference names; oracle/lapack_lu.c
+# (own code) defines the two real ones where a build links them
+LAPACKE_STUB = ("/* stub lapacke.h: declares the LAPACK routines the reference names */\n"
+                "void LAPACK_zgetrf(int* m, int* n, _Complex double* a, int* lda, int* ipiv, int* info);\n"
+                "void LAPACK_dgetrf(int* m, int* n, double* a, int* lda, int* ipiv, int* info);\n"
+                "void LAPACK_dgetri(int* n, double* a, int* lda, int* ipiv, double* work, int* lwork, int* info);\n")
+
+
 def generate_vecops() -> None:
-    """The fermion-bag operator: vec_ops.c unchanged, next to a copy of
-    Thirring.h whose ``#define NT 64`` / ``#define NX 64`` become REF_NT / REF_NX
-    (vec_ops.c includes "Thirring.h" from its own directory, so both sit in
-    oracle/_ref/src/vecops/)."""
+    """The fermion-bag sources: vec_ops.c, fermion_matrix.c and full_determinant.c
+    unchanged, next to a copy of Thirring.h with these edits (every file
+    includes "Thirring.h" from its own directory, so all sit in
+    oracle/_ref/src/vecops/):
+
+      * ``#define NT 64`` / ``#define NX 64``  ->  REF_NT / REF_NX;
+      * ``#define ANTISYMMETRIC`` is kept unless REF_OPENX is set, which selects
+        the file's own OPENX boundary instead (open x, antisymmetric t);
+      * ``#define FLUCTUATION_MATRIX`` is kept unless REF_NO_FLUCTUATION_MATRIX
+        is set: full_determinant.c compiles its determinant_mu only without it
+        (full_determinant.c:15).
+    """
     os.makedirs(VSRC, exist_ok=True)
     with open(os.path.join(REF_ROOT, "Thirring.h")) as f:
         text = f.read()
     text = _sub(r"^#define NT 64\s*$", "#define NT REF_NT", text, 1, re.M)
     text = _sub(r"^#define NX 64\s*$", "#define NX REF_NX", text, 1, re.M)
+    text = _sub(r"^#define ANTISYMMETRIC //Antisymmetric boundaries\s*$",
+                "#if REF_OPENX\n#define OPENX\n#else\n#define ANTISYMMETRIC //Antisymmetric boundaries\n#endif",
+                text, 1, re.M)
+    text = _sub(r"^#define FLUCTUATION_MATRIX\s*$",
+                "#ifndef REF_NO_FLUCTUATION_MATRIX\n#define FLUCTUATION_MATRIX\n#endif", text, 1, re.M)
     with open(os.path.join(VSRC, "Thirring.h"), "w") as f:
         f.write("/* GENERATED by oracle/make_ref.py from rantahar/Thirring2D Thirring.h -- do not commit. */\n" + text)
-    for name in ("vec_ops.c", "fermion_matrix.c", "mersenne_inline.c", "mersenne.h"):
+    for name in ("vec_ops.c", "fermion_matrix.c", "full_determinant.c", "mersenne_inline.c", "mersenne.h"):
         with open(os.path.join(REF_ROOT, name)) as fi, open(os.path.join(VSRC, name), "w") as fo:
             fo.write(fi.read())
     with open(os.path.join(VSRC, "lapacke.h"), "w") as f:
-        f.write("void LAPACK_zgetrf(int* m, int* n, _Complex double* a, int* lda, int* ipiv, int* info);\n")
+        f.write(LAPACKE_STUB)
+
+
+BSRC = os.path.join(SRC, "brute")
+
+
+def generate_brute() -> None:
+    """tests/thirring_brute.c, the reference's brute-force enumeration of the
+    fermion-bag partition function on 4 x 4 with open x (its header fixes the
+    size and boundary), with two edits:
+
+      * ``#include "test_thirring.h"`` -> ``#include "thirring_brute.h"``: the
+        header the repository ships under that other name (thirring_brute.c:10);
+      * the final table's ``%g`` -> ``%.17g`` (five fields of one printf), so the
+        sums come out at full precision.
+
+    thirring_brute.h is copied unchanged; its ``#include "../mersenne.h"``
+    finds oracle/_ref/src/mersenne.h, and its <lapacke.h> the stub here.
+    """
+    os.makedirs(BSRC, exist_ok=True)
+    with open(os.path.join(REF_ROOT, "tests", "thirring_brute.c")) as f:
+        text = f.read()
+    text = _sub(r'#include "test_thirring\.h"', '#include "thirring_brute.h"', text, 1)
+    lines = text.split("\n")
+    hits = [i for i, ln in enumerate(lines) if 'printf(" Links %d Monomers %d det %g' in ln]
+    if len(hits) != 1:
+        raise RuntimeError(f"make_ref: brute-force table printf found {len(hits)} times, expected 1")
+    lines[hits[0]] = _sub(r"%g", "%.17g", lines[hits[0]], 5)
+    with open(os.path.join(BSRC, "thirring_brute.c"), "w") as f:
+        f.write("/* GENERATED by oracle/make_ref.py from rantahar/Thirring2D tests/thirring_brute.c -- do not "
+                "commit. */\n" + "\n".join(lines))
+    with open(os.path.join(REF_ROOT, "tests", "thirring_brute.h")) as fi, \
+            open(os.path.join(BSRC, "thirring_brute.h"), "w") as fo:
+        fo.write(fi.read())
+    with open(os.path.join(BSRC, "lapacke.h"), "w") as f:
+        f.write(LAPACKE_STUB)
+
+
+def brute_path() -> str:
+    return os.path.join(OUT, "thirring_brute_T4X4")
+
+
+def build_brute() -> str:
+    """The brute-force program (reads its parameters from stdin as the
+    reference's does), with vec_ops.c at 4 x 4 and open x for its
+    measure_charge, and oracle/lapack_lu.c for dgetrf/dgetri."""
+    out = brute_path()
+    srcs = [os.path.join(BSRC, "thirring_brute.c"), os.path.join(VSRC, "vec_ops.c"),
+            os.path.join(SRC, "mersenne_inline.c"), os.path.join(HERE, "lapack_lu.c")]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(s) for s in srcs):
+        return out
+    cmd = (["gcc", "-O2", "-std=gnu99", "-w", "-fcommon", f"-I{BSRC}", f"-I{VSRC}", "-DREF_NT=4", "-DREF_NX=4",
+            "-DREF_OPENX=1", "-o", out] + srcs + ["-lm"])
+    subprocess.run(cmd, check=True)
+    return out
+
+
+DET_SIZES = [(4, 4)]
+
+
+def det_lib_path(nt: int, nx: int, openx: bool) -> str:
+    return os.path.join(OUT, f"libdetref_T{nt}X{nx}_{'openx' if openx else 'apx'}.so")
+
+
+def build_det_one(nt: int, nx: int, openx: bool) -> str:
+    """full_determinant.c's determinant_mu with fermion_matrix.c's fM_index
+    (mass on the diagonal), FLUCTUATION_MATRIX undefined, driven by
+    oracle/det_driver.c; fermion_matrix.c and the driver both define the
+    neighbour tables, hence -fcommon."""
+    out = det_lib_path(nt, nx, openx)
+    srcs = [os.path.join(HERE, "det_driver.c"), os.path.join(VSRC, "full_determinant.c"),
+            os.path.join(VSRC, "fermion_matrix.c"), os.path.join(HERE, "lapack_lu.c")]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(s) for s in srcs):
+        return out
+    cmd = (["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", "-w", "-fcommon", "-Wl,-Bsymbolic", f"-I{VSRC}",
+            f"-DREF_NT={nt}", f"-DREF_NX={nx}", f"-DREF_OPENX={1 if openx else 0}", "-DREF_NO_FLUCTUATION_MATRIX",
+            "-o", out] + srcs + ["-lm"])
+    subprocess.run(cmd, check=True)
+    return out
 
 
 def vec_lib_path(nt: int, nx: int) -> str:
@@ -226,6 +325,7 @@ def build(sizes=None, variants=None) -> list[str]:
     if os.path.exists(os.path.join(REF_ROOT, "hmc.c")):
         generate()
         generate_vecops()
+        generate_brute()
     elif not os.path.exists(os.path.join(SRC, "hmc_patched.c")):
         return []
     sizes = sizes or DEFAULT_SIZES
@@ -238,6 +338,11 @@ def build(sizes=None, variants=None) -> list[str]:
             libs += list(ex.map(lambda j: build_vec_one(*j), VEC_SIZES))
         if os.path.exists(os.path.join(VSRC, "fermion_matrix.c")):
             libs += list(ex.map(lambda j: build_prop_one(*j), PROP_SIZES))
+        if os.path.exists(os.path.join(VSRC, "full_determinant.c")):
+            libs += list(ex.map(lambda j: build_det_one(*j), [(nt, nx, o) for (nt, nx) in DET_SIZES
+                                                              for o in (False, True)]))
+        if os.path.exists(os.path.join(BSRC, "thirring_brute.c")):
+            libs.append(build_brute())
     return libs
 
 

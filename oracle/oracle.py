@@ -317,6 +317,10 @@ class RefHMC:
         self.L.ref_trajectory(nsteps, C.c_double(tau), _ptr(stats))
         return stats
 
+    def update_gauge(self):
+        """The reference's own update_gauge(A) (hmc.c:671-746; prints to stdout)."""
+        self.L.ref_update_gauge()
+
 
 def _ref_dense(self):
     """hmc.c fermion_matrix as a row-major complex [V, V] array (M psi = Md @ psi)."""
@@ -381,3 +385,65 @@ class RefVecOps:
         finally:
             os.chdir(cwd)
         return out
+
+
+# ---------------------------------------------------------------------------
+# The reference's determinant code (oracle/_ref), when it has been built.
+# ---------------------------------------------------------------------------
+class RefFullDet:
+    """A private instance of the reference's full_determinant.c determinant_mu
+    (full_determinant.c:144-186) over fermion_matrix.c's fM_index with the mass
+    on the diagonal, on 4 x 4 (antisymmetric boundaries, or open x)."""
+
+    def __init__(self, nt, nx, m, mu, openx):
+        from oracle import make_ref
+        src = make_ref.det_lib_path(nt, nx, openx)
+        if not os.path.exists(src):
+            raise FileNotFoundError(f"{src} not built (python oracle/make_ref.py)")
+        self._tmp = tempfile.mkdtemp(prefix="detref_")
+        path = os.path.join(self._tmp, os.path.basename(src))
+        shutil.copy(src, path)
+        self.L = C.CDLL(path)
+        self.L.dref_determinant_mu.restype = C.c_double
+        self.nt, self.nx, self.mu = nt, nx, mu
+        self.L.dref_setup(C.c_double(m), C.c_double(mu))
+
+    def __del__(self):
+        shutil.rmtree(getattr(self, "_tmp", ""), ignore_errors=True)
+
+    def determinant(self, mask=None):
+        """det of fM_index over the sites with mask == 0 (all sites by default)."""
+        mask = np.zeros((self.nt, self.nx), np.int32) if mask is None else mask
+        self.L.dref_set_field(_ptr(np.ascontiguousarray(mask, dtype=np.int32), _ip))
+        return self.L.dref_determinant_mu(C.c_double(self.mu))
+
+
+def ref_brute(mu: float, m: float = 0.0, U: float = 1.0, seed: int = 54357345) -> dict:
+    """Run the reference's brute-force enumeration (tests/thirring_brute.c, 4 x 4,
+    open x) and parse its table: arrays [links, monomers] of the sums of det,
+    |det|, det*charge, det*chiralcharge and det*chiralsusc."""
+    import re
+    from oracle import make_ref
+    exe = make_ref.brute_path()
+    if not os.path.exists(exe):
+        raise FileNotFoundError(f"{exe} not built (python oracle/make_ref.py)")
+    work = tempfile.mkdtemp(prefix="brute_")
+    try:
+        r = subprocess.run([exe], input=f"1000000\n1\n100\n{float(m)!r}\n{float(U)!r}\n{float(mu)!r}\n{int(seed)}\n",
+                           text=True, capture_output=True, cwd=work, timeout=3600)
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    if f" mu {float(mu):f} " not in r.stdout:
+        raise RuntimeError("brute-force run did not read mu: " + r.stdout[:500])
+    rows = re.findall(r"Links (\d+) Monomers (\d+) det (\S+) abs\(det\) (\S+) det\*charge (\S+) "
+                      r"det\*chiralcharge (\S+) det\*chiralsusc (\S+)", r.stdout)
+    if not rows or "simulation done" not in r.stdout:
+        raise RuntimeError("brute-force run failed: " + r.stdout[-500:] + r.stderr[-500:])
+    nl = max(int(x[0]) for x in rows) + 1
+    nm = max(int(x[1]) for x in rows) + 1
+    out = {k: np.zeros((nl, nm)) for k in ("det", "absdet", "charge", "chiralcharge", "chiralsusc")}
+    for row in rows:
+        i, j = int(row[0]), int(row[1])
+        for k, v in zip(("det", "absdet", "charge", "chiralcharge", "chiralsusc"), row[2:]):
+            out[k][i, j] = float(v)
+    return out

@@ -170,8 +170,47 @@ def make_prop():
                             Dinv=ref.calc_Dinv())
 
 
+def make_determinant_pins():
+    """The reference's own determinant code on 4 x 4 (its brute-force test size):
+
+      * full_determinant.c's determinant_mu over fermion_matrix.c's fM_index
+        (mass on the diagonal), antisymmetric boundaries and open x, for several
+        m and mu, on the empty field (det(m + D) at A = 0) and on two monomer
+        masks (the determinant over the unoccupied sites);
+      * tests/thirring_brute.c's enumeration (open x) at three mu: the sums of
+        the fermion-bag weights per (links, monomers).  With no links they give
+        det(m + D) = sum_k m^k Z[0][k] / Z[0][16] for every m (the
+        principal-minor expansion of det(m + D) with Jacobi's identity).
+    """
+    from oracle.oracle import RefFullDet, ref_brute
+    nt = nx = 4
+    rng = np.random.default_rng(44)
+    masks = np.stack([np.zeros((nt, nx), np.int32)] +
+                     [(rng.random((nt, nx)) < 0.3).astype(np.int32) for _ in range(2)])
+    pairs = [(0.1, 0.0), (0.3, 0.1), (0.05, 0.25), (1.0, 0.0)]
+    dets = np.zeros((2, len(pairs), len(masks)))
+    for b, openx in enumerate((False, True)):
+        for i, (m, mu) in enumerate(pairs):
+            ref = RefFullDet(nt, nx, m, mu, openx)
+            for k, mask in enumerate(masks):
+                dets[b, i, k] = ref.determinant(mask)
+    np.savez_compressed(os.path.join(OUT, "fulldet_4x4.npz"), nt=nt, nx=nx, boundaries=np.array(["apx", "openx"]),
+                        m_mu=np.array(pairs), masks=masks, det=dets)
+    mus = np.array([0.1, 0.0, 0.3])
+    runs = [ref_brute(float(mu)) for mu in mus]
+    Z = np.stack([r["det"] for r in runs])
+    Zabs = np.stack([r["absdet"] for r in runs])
+    np.savez_compressed(os.path.join(OUT, "brute_4x4_openx.npz"), nt=nt, nx=nx, mu=mus, Z=Z, Zabs=Zabs)
+    print("fulldet", dets[:, :, 0], "brute Z[0]", Z[:, 0, :])
+
+
 if __name__ == "__main__":
-    # no arguments: every fixture; else only the named trajectory configs
+    # no arguments: every fixture; "determinants": the determinant pins only;
+    # else only the named trajectory configs
+    if sys.argv[1:] == ["determinants"]:
+        make_ref.build([(4, 4)])
+        make_determinant_pins()
+        sys.exit(0)
     names = sys.argv[1:] or list(CONFIGS)
     make_ref.build(sorted({(CONFIGS[n][0], CONFIGS[n][1]) for n in names} | {(4, 4), (6, 4)}))
     if not sys.argv[1:]:
@@ -180,5 +219,6 @@ if __name__ == "__main__":
         make_prop()
         make_mt()
         make_dense()
+        make_determinant_pins()
     for name in names:
         make_config(name, *CONFIGS[name])
