@@ -150,3 +150,33 @@ def test_grid_barrier_gives_up_and_device_stays_usable(tg):
     assert res.status == 0
     r = b - L.fm_conjugate_mul(L.fm_mul(x))
     assert np.linalg.norm(r) < 2e-10 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("nt,nx,mu,m,tol", [(64, 64, 0.0, 0.1, 1e-10), (32, 96, 0.3, 0.2, 1e-12), (256, 256, 0.0, 0.05, 1e-10),
+                                            (4, 32, 0.0, 0.3, 1e-10), (1024, 1024, 0.0, 0.05, 1e-10)])
+def test_single_reduction_mixed_cg(tg, oracle_lib, monkeypatch, nt, nx, mu, m, tol):
+    """The mixed persistent solve on column-march lattices runs as the
+    single-reduction CG (one grid sum and one fused M^dag M pass per
+    iteration).  Against the two-sum form (TG_MIXED_CG=twosum) on the same
+    system: the same status, iteration counts within 2%, solutions within the
+    tolerance's reach, and the true residual |b - M^dag M x| / |b| (oracle, FP64)
+    below the target."""
+    rng = np.random.default_rng(nt + 7 * nx)
+    A = rng.normal(0, 0.3, (nt, nx, 2))
+    b = cplx(rng, (nt, nx))
+    cp = tg.cg_params(rel_tol=tol, abs_tol2=0, precision=tg.native.PREC_MIXED, ru_interval=50, solver=PERSISTENT)
+    out = {}
+    for form in ("twosum", "onesum"):
+        monkeypatch.setenv("TG_MIXED_CG", form)
+        L = tg.Lattice(nt, nx, m, 0.5, mu, -1, 1)
+        L.set_gauge(A)
+        out[form] = L.fmdm_invert_cg(b, cp)
+        L.close()
+    (x2, r2), (x1, r1) = out["twosum"], out["onesum"]
+    assert r1.status == r2.status == 0
+    assert abs(r1.iterations - r2.iterations) <= max(2, r2.iterations // 50), (r1.iterations, r2.iterations)
+    assert r1.reliable_updates >= 1
+    assert rel(x1, x2) < 100 * tol
+    o = oracle_lib.Oracle(nt, nx, m, 0.5, mu, -1, 1)
+    true = np.linalg.norm(b - o.Mdag(A, o.M(A, x1))) / np.linalg.norm(b)
+    assert true < 1.5 * tol, true

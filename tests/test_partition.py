@@ -140,3 +140,65 @@ def test_ranges_differ_by_at_most_one_row():
     for nw in (2432, 2433, 4864):
         sizes = [rows * (w + 1) // nw - rows * w // nw for w in range(nw)]
         assert max(sizes) - min(sizes) <= 1 and sum(sizes) == rows
+
+
+def fused_segment_accesses(nt, nx, xw, ta, tb):
+    """march_mdagm (thirring2d_gb300/csrc/tg_fused.cuh): (reads, writes) of one
+    warp's segment -- v and the links at rows ta-2 .. tb+1 of its columns, the
+    operands beyond its edges, and the five v and four links of every
+    recomputed edge u."""
+    V = nt * nx
+    x0 = xw << 5
+    xle = nx - 1 if x0 == 0 else x0 - 1
+    xre = 0 if x0 + 32 == nx else x0 + 32
+
+    def wrap(t):
+        assert -nt <= t < 2 * nt
+        return t + nt if t < 0 else (t - nt if t >= nt else t)
+
+    def u_at(t, c):
+        tp, tm = wrap(t + 1), wrap(t - 1)
+        cp, cm = (0 if c + 1 == nx else c + 1), (nx - 1 if c == 0 else c - 1)
+        return [t * nx + c, tp * nx + c, tm * nx + c, t * nx + cp, t * nx + cm, t * nx + c, tm * nx + c, t * nx + c,
+                t * nx + cm]
+
+    reads, writes = [], []
+    cols = [x0 + lane for lane in range(32)]
+    for r in (wrap(ta - 2), wrap(ta - 1), ta, wrap(ta + 1)):    # prologue: v, Wt, Wx
+        reads += [r * nx + c for c in cols]
+    for r in (wrap(ta - 1), ta):                                  # prologue edges (lanes 0 and 31)
+        reads += [r * nx + xle, r * nx + xre]
+    t = ta
+    while t + K_MARCH_T <= tb:
+        for i in range(K_MARCH_T):
+            reads += [wrap(t + 2 + i) * nx + c for c in cols] + [wrap(t + 1 + i) * nx + c for c in cols]
+            for c in (xle, xre):
+                reads.append(wrap(t + 1 + i) * nx + c)
+                reads += u_at(t + i, c)
+            writes += [(t + i) * nx + c for c in cols]
+        t += K_MARCH_T
+    while t < tb:
+        reads += [wrap(t + 2) * nx + c for c in cols] + [wrap(t + 1) * nx + c for c in cols]
+        for c in (xle, xre):
+            reads.append(wrap(t + 1) * nx + c)
+            reads += u_at(t, c)
+        writes += [t * nx + c for c in cols]
+        t += 1
+    assert all(0 <= a < V for a in reads), "read outside the lattice"
+    return writes
+
+
+@pytest.mark.parametrize("nt,nx", SHAPES)
+def test_fused_march_partition_writes_each_site_once(nt, nx):
+    """The fused M^dag M march over the persistent solver's grid shapes: every
+    site written by exactly one warp and lane per pass, every read inside the
+    lattice (the halo rows and edge columns wrap)."""
+    if nt < 2:
+        return
+    for grid, wpb in ((1, 8), (4, 16), (152, 16), (304, 8)):
+        V = nt * nx
+        count = [0] * V
+        for _, xw, ta, tb in warp_segments_grid(nt, nx, grid, wpb):
+            for s in fused_segment_accesses(nt, nx, xw, ta, tb):
+                count[s] += 1
+        assert min(count) == 1 and max(count) == 1

@@ -80,14 +80,16 @@ def test_reference_arm_reports_the_whole_host(capsys, monkeypatch):
     Ctx.Pool = Pool
     seen = []
 
-    def host_sample(pool, cores, seconds, seed):
+    def host_sample(pool, cores, seconds, seed, iters_per_traj):
         seen.append((pool.n, cores, seed))
+        assert iters_per_traj == 300 * bench.SOLVES_PER_TRAJ
         return 0.004 + 0.001 * len(seen), "reference"
     monkeypatch.setattr(multiprocessing, "get_context", lambda kind: Ctx)
     monkeypatch.setattr(bench, "host_cores", lambda: 4)
     monkeypatch.setattr(bench, "cpu_host_sample", host_sample)
+    monkeypatch.setattr(bench, "host_iteration_count", lambda: 300)
     monkeypatch.setattr(bench, "cpu_sample",
-                        lambda repeats=1: dict(value=0.001, kind="reference", cores=1, sample="one core"))
+                        lambda iters, repeats=1: dict(value=0.001, kind="reference", cores=1, sample="one core"))
 
     class Args:
         steps, warmup, gpus = 3, 1, 1
@@ -97,6 +99,7 @@ def test_reference_arm_reports_the_whole_host(capsys, monkeypatch):
     assert len(seen) == 4 and all(n == 4 and c == 4 for n, c, _ in seen)
     assert len({s for _, _, s in seen}) == 4                       # fresh fields every step
     assert line["value"] == pytest.approx(statistics.median([0.006, 0.007, 0.008]))
+    assert line["cg_iterations"]["first_solve_counted_on_host"] == 300
     cb = line["cpu_baseline"]
     assert cb["cores"] == 4 and cb["value"] == line["value"] and cb["kind"] == "reference"
     assert cb["single_process"] == {"value": 0.001, "cores": 1, "kind": "reference", "sample": "one core"}

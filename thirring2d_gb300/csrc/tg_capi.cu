@@ -124,7 +124,7 @@ struct tg_lattice {
   TrajStats* ts = nullptr;
   Red red{};
   unsigned* bar = nullptr;      // persistent solver: grid barrier {count, gen}
-  double* pcg_part = nullptr;   // and its partial sums [2 * kPcgMaxGrid]
+  double* pcg_part = nullptr;   // and its partial sums [4 * kPcgMaxGrid]
 
   double* h_stage = nullptr;  // pinned, 2*V*kMaxPf doubles... sized at create
   size_t h_stage_len = 0;
@@ -285,6 +285,17 @@ bool use_persistent(const tg_cg_params& cp) {
   return kDefaultPersistent;
 }
 
+// The mixed persistent solve runs the two-sum CG (k_pcgmx) by default;
+// TG_MIXED_CG=onesum selects, on column-march lattices, the single-reduction
+// CG (k_pcgcg: one grid sum and one fused M^dag M pass per iteration), which
+// measured slower on GB300 (1024^2: 27.7 against 21.8 us per iteration; 2048^2:
+// 122 against 103 us): its fused pass is latency-bound.
+bool use_single_reduction(const tg_lattice* L) {
+  if (!L->g.march) return false;
+  const char* e = getenv("TG_MIXED_CG");
+  return e && strcmp(e, "onesum") == 0;
+}
+
 // The whole solve as one cooperative launch (tg_pcg.cu); the barrier's
 // arrival count is cleared first, so a solve that timed out leaves no trace.
 int enqueue_pcg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const double2* b, double2* x, int log_index) {
@@ -320,7 +331,16 @@ int enqueue_pcg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const dou
     a.abs_tol2 = cp.abs_tol2;
     a.maxiter = cp.maxiter;
     a.ru_interval = cp.ru_interval;
-    e = pcgmx(s, L->P.mu == 0.0, a);
+    if (use_single_reduction(L)) {
+      a.r1 = L->wmx.ps[1];
+      a.w0 = L->wmx.Mps;
+      a.w1 = L->wmx.xtra[0];
+      a.s0 = L->wmx.xtra[1];
+      a.s1 = L->wmx.xtra[2];
+      e = pcgcg(s, L->P.mu == 0.0, a);
+    } else {
+      e = pcgmx(s, L->P.mu == 0.0, a);
+    }
   } else {
     Pcg64Args a{};
     a.g = L->g;
@@ -765,13 +785,14 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
                     &L->w64.r, &L->w64.p[0], &L->w64.p[1], &L->w64.Mp, &L->wmx.tmp64};
   for (auto pp : d2)
     if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
-  float2** f2[] = {&L->Wt32, &L->Wx32, &L->wmx.xs, &L->wmx.rs, &L->wmx.ps[0], &L->wmx.ps[1], &L->wmx.Mps};
+  float2** f2[] = {&L->Wt32, &L->Wx32, &L->wmx.xs, &L->wmx.rs, &L->wmx.ps[0], &L->wmx.ps[1], &L->wmx.Mps,
+                   &L->wmx.xtra[0], &L->wmx.xtra[1], &L->wmx.xtra[2]};
   for (auto pp : f2)
     if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
   if ((rc = dmalloc(&L->st, 1)) != TG_OK || (rc = dmalloc(&L->log, kMaxLog)) != TG_OK ||
       (rc = dmalloc(&L->ts, 1)) != TG_OK || (rc = dmalloc(&L->red.partials, (size_t)nblocks((int)V) + 32)) != TG_OK ||
       (rc = dmalloc(&L->red.counter, 1)) != TG_OK || (rc = dmalloc(&L->bar, 2)) != TG_OK ||
-      (rc = dmalloc(&L->pcg_part, 2 * (size_t)kPcgMaxGrid)) != TG_OK)
+      (rc = dmalloc(&L->pcg_part, 4 * (size_t)kPcgMaxGrid)) != TG_OK)
     return bail(rc);
   if ((rc = ensure_pf(L, 1)) != TG_OK) return bail(rc);
   L->h_stage_len = (size_t)(kMaxPf + 2) * 2 * n;  // npf eta fields + momenta + noise
@@ -806,7 +827,7 @@ int tg_destroy(tg_lattice* L) {
   for (auto e : L->ev) cudaEventDestroy(e);
   void* dev[] = {L->A, L->Anew, L->Wt, L->Wx, L->Wt1, L->Wx1, L->mom, L->noise, L->chi, L->Mchi, L->vin, L->vout, L->w64.r,
                  L->w64.p[0], L->w64.p[1], L->w64.Mp, L->wmx.tmp64, L->Wt32, L->Wx32, L->wmx.xs, L->wmx.rs,
-                 L->wmx.ps[0], L->wmx.ps[1], L->wmx.Mps,
+                 L->wmx.ps[0], L->wmx.ps[1], L->wmx.Mps, L->wmx.xtra[0], L->wmx.xtra[1], L->wmx.xtra[2],
                  L->st, L->log, L->ts, L->red.partials, L->red.counter, L->bar, L->pcg_part, L->eta, L->phi, L->unif, L->mask,
                  L->rv[0], L->rv[1], L->rv[2], L->rv[3], L->rv[4], L->rv[5]};
   for (void* d : dev)

@@ -20,6 +20,7 @@ struct CgBufs64 {          // FP64 CG work vectors (p alternates between two buf
 struct CgBufsMixed {       // FP32 CG work vectors + FP64 accumulators
   float2 *xs, *rs, *ps[2], *Mps;
   double2* tmp64;          // M x for the reliable update
+  float2* xtra[3];         // single-reduction CG: its second r, second w and two s buffers with ps[1], Mps
 };
 
 struct Red {               // reduction scratch
@@ -118,7 +119,9 @@ void lu_logdet(cudaStream_t s, int V, int nmat, double2* mats, double* out);
 struct GridBar {       // grid barrier: monotonic arrival count (must be 0 at launch)
   unsigned* count;
 };
-constexpr int kPcgMaxGrid = 4096;  // partial sums: 2 * kPcgMaxGrid doubles
+// largest persistent grid; partial sums: 4 * kPcgMaxGrid doubles (two alternating
+// arrays of (gamma, delta) pairs in the single-reduction CG)
+constexpr int kPcgMaxGrid = 4096;
 
 struct Pcg64Args {
   Geo g;
@@ -145,6 +148,8 @@ struct PcgMxArgs {
   const double2* b;
   double2 *x, *tmp;
   float2 *xs, *r, *p0, *p1, *Mp;
+  // single-reduction CG (k_pcgcg): r alternates r/r1, w w0/w1, s s0/s1; p0 is p
+  float2 *r1, *w0, *w1, *s0, *s1;
   CgState* st;
   CgLog* log;
   int log_index;
@@ -156,6 +161,9 @@ struct PcgMxArgs {
 
 cudaError_t pcg64(cudaStream_t s, bool mu0, Pcg64Args a);
 cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a);
+// the mixed solve as a single-reduction CG whose pass applies M^dag M in one
+// column march (lattices with g.march only); same arguments and results
+cudaError_t pcgcg(cudaStream_t s, bool mu0, PcgMxArgs a);
 // one grid barrier (4 blocks, cooperative) that also waits for `phantom` absent
 // blocks, giving up after `limit` polls: *status = TG_OK or TG_E_TIMEOUT
 cudaError_t barrier_check(cudaStream_t s, unsigned* count, unsigned phantom, long long limit, int* status);

@@ -23,7 +23,7 @@
 #include <mutex>
 #include <unordered_map>
 
-#include "tg_stencil.cuh"
+#include "tg_fused.cuh"
 
 namespace tg {
 
@@ -255,8 +255,10 @@ template <int BS, bool MU0>
 __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
   if (threadIdx.x == 0) barrier_epoch() = 0;
   const Geo& g = a.g;
+  // consecutive sums never share an array: alpha A, beta B, reliable update C
   double* partA = a.part;
   double* partB = a.part + gridDim.x;
+  double* partC = a.part + 2 * gridDim.x;
   double v = 0;
   TG_SITES(s, g.V) {
     const double2 bb = a.b[s];
@@ -361,7 +363,7 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
     };
     stencil_ld<double, 1, MU0>(g, a.kd, ld_t, a.Wt, a.Wx, epi_t);
     double rt;
-    if (!grid_total<BS>(vt, partA, a.bar, rt)) {
+    if (!grid_total<BS>(vt, partC, a.bar, rt)) {
       status = TG_E_TIMEOUT;
       break;
     }
@@ -374,6 +376,261 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
     else if (rt < stop) status = TG_OK;
     else if (rt / rr0 > 1e10) status = TG_E_DIVERGED;
     else if (iter >= a.maxiter) status = TG_E_NOCONV;
+  }
+  pcg_report(a.st, a.log, a.log_index, rr, rr0, stop, iter, n_ru, status);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed, single reduction: the same solve as k_pcgmx (FP32 iterations, FP64
+// reliable updates with the same triggers and restart rule, the same stopping
+// tests), with CG in the Chronopoulos-Gear form (A. T. Chronopoulos and
+// C. W. Gear, J. Comput. Appl. Math. 25 (1989) 153): with A = M^dag M,
+//   s_k = w_k + beta_k s_{k-1},  p_k = r_k + beta_k p_{k-1},
+//   x_{k+1} = x_k + alpha_k p_k,  r_{k+1} = r_k - alpha_k s_k,  w_{k+1} = A r_{k+1},
+//   gamma = (r_{k+1}, r_{k+1}),  delta = (r_{k+1}, A r_{k+1}) = |M r_{k+1}|^2,
+//   beta_{k+1} = gamma / gamma_k,  alpha_{k+1} = gamma / (delta - beta_{k+1} gamma / alpha_k),
+// so one grid sum (gamma and delta together) per iteration instead of two.
+// Each iteration is one pass of the fused M^dag M march (tg_fused.cuh): the
+// loader forms s_k and r_{k+1} where it reads, at every site including the
+// halo, and the epilogue stores r_{k+1}, s_k, w_{k+1}, p_k and x_{k+1}.  r, s
+// and w alternate between two buffers (halo sites of other warps are still
+// read while a pass writes); p and x are only read where they are written.
+// Column-march lattices only (nx a multiple of 32, nt of kMarchT).
+// ---------------------------------------------------------------------------
+struct CgcgOp {
+  float2 v, sk;  // r_{k+1}, s_k at one site (the epilogue reads r_k again: registers)
+};
+__device__ __forceinline__ float2 axpy2(float a, float2 x, float2 y) {
+  return make_float2(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y));
+}
+struct CgcgLd {  // r_{k+1} = r_k - alpha_k (w_k + beta_k s_{k-1}) on the fly
+  using Op = CgcgOp;
+  const float2 *r, *w, *sp;
+  float al, be;
+  __device__ __forceinline__ Op own(int i) const {
+    const float2 rv = __ldcg(r + i), wv = __ldcg(w + i), sv = __ldcg(sp + i);
+    const float2 sk = axpy2(be, sv, wv);
+    return Op{axpy2(-al, sk, rv), sk};
+  }
+  __device__ __forceinline__ float2 val(int i) const { return own(i).v; }
+};
+struct PlainOp {
+  float2 v;
+};
+struct PlainLd {  // the vector itself (the first w = A r, and after a reliable update)
+  using Op = PlainOp;
+  const float2* r;
+  __device__ __forceinline__ Op own(int i) const { return Op{__ldcg(r + i)}; }
+  __device__ __forceinline__ float2 val(int i) const { return __ldcg(r + i); }
+};
+
+// The grid total of a pair of partials (gamma, delta): FP32 within a block, FP64
+// across blocks in index order, handed to f in thread 0 of every block.
+template <int BS, class F>
+__device__ __forceinline__ bool grid_total2_then(float va, float vb, double* part, const GridBar& bar, F f,
+                                                 decltype(f(0.0, 0.0))& out) {
+  using S = decltype(f(0.0, 0.0));
+  __shared__ float sha[BS / 32], shb[BS / 32];
+  __shared__ double sda[BS / 32], sdb[BS / 32];
+  __shared__ S s_out;
+  va = warp_sum(va);
+  vb = warp_sum(vb);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sha[wid] = va;
+    shb[wid] = vb;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    float a = (lane < BS / 32) ? sha[lane] : 0.f, b = (lane < BS / 32) ? shb[lane] : 0.f;
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if (lane == 0) {
+      part[2 * blockIdx.x] = (double)a;
+      part[2 * blockIdx.x + 1] = (double)b;
+    }
+  }
+  if (!grid_barrier(bar)) return false;
+  double a = 0, b = 0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += BS) {
+    a += __ldcg(part + 2 * i);
+    b += __ldcg(part + 2 * i + 1);
+  }
+  a = warp_sum(a);
+  b = warp_sum(b);
+  if (lane == 0) {
+    sda[wid] = a;
+    sdb[wid] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0, tb = 0;
+    for (int k = 0; k < BS / 32; k++) {
+      ta += sda[k];
+      tb += sdb[k];
+    }
+    s_out = f(ta, tb);
+  }
+  __syncthreads();
+  out = s_out;
+  return true;
+}
+
+struct CgcgScal {
+  double gam, alpha, beta;
+  int need;  // a reliable update is due
+};
+
+template <int BS, bool MU0>
+__global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgcg(PcgMxArgs a) {
+  if (threadIdx.x == 0) barrier_epoch() = 0;
+  const Geo& g = a.g;
+  // Partial sums: two arrays of 2 * grid doubles (pairs; a single sum uses the
+  // first half), used strictly in turn: a block that runs ahead to the next sum
+  // writes the other array, never one that a slower block is still reading.
+  int nsum = 0;
+  auto part = [&]() { return a.part + 2 * gridDim.x * ((nsum++) & 1); };
+  double v = 0;
+  TG_SITES(s, g.V) {  // x = 0, r_0 = b, p_{-1} = s_{-1} = 0
+    const double2 bb = a.b[s];
+    a.x[s] = make_double2(0.0, 0.0);
+    a.xs[s] = make_float2(0.f, 0.f);
+    a.r[s] = make_float2((float)bb.x, (float)bb.y);
+    a.p0[s] = make_float2(0.f, 0.f);
+    a.s1[s] = make_float2(0.f, 0.f);
+    v = fma(bb.x, bb.x, v);
+    v = fma(bb.y, bb.y, v);
+  }
+  double rr = 0;
+  int status = -1, iter = 0, n_ru = 0, since_ru = 0;
+  if (!grid_total<BS>(v, part(), a.bar, rr)) status = TG_E_TIMEOUT;
+  const double rr0 = rr;
+  const double stop = stop_of(rr0, a.rel_tol, a.abs_tol2);
+  double rr_true = rr;
+  if (status < 0) {
+    if (isnan(rr)) status = TG_E_NAN;
+    else if (!(rr >= stop) || rr == 0.0) status = TG_OK;
+  }
+  // w_0 = A r_0; gamma_0, delta_0
+  double gam = 0, del = 0, alpha = 0, beta = 0;
+  auto first_w = [&](float2* r, float2* w) -> bool {  // w = A r; gam, del = (r, r), (r, A r)
+    float ga = 0.f, de = 0.f;
+    const PlainLd ld{r};
+    auto epi = [&](int s, float2 wv, float2 u, const PlainOp& o) {
+      w[s] = wv;
+      ga = fmaf(o.v.x, o.v.x, fmaf(o.v.y, o.v.y, ga));
+      de = fmaf(u.x, u.x, fmaf(u.y, u.y, de));
+    };
+    stencil_mdagm<MU0>(g, a.km32, a.kd32, ld, a.Wt32, a.Wx32, epi);
+    double2 gd;
+    if (!grid_total2_then<BS>(ga, de, part(), a.bar, [](double x, double y) { return make_double2(x, y); }, gd))
+      return false;
+    gam = gd.x;
+    del = gd.y;
+    return true;
+  };
+  if (status < 0) {
+    if (first_w(a.r, a.w0)) alpha = gam / del;
+    else status = TG_E_TIMEOUT;
+  }
+  while (status < 0) {
+    const bool odd = iter & 1;
+    const float af = (float)alpha, bf = (float)beta;
+    const float2* const rc = odd ? a.r1 : a.r;   // r_k
+    float2* const rn = odd ? a.r : a.r1;          // r_{k+1}
+    float2* const wn = odd ? a.w0 : a.w1;         // w_{k+1}
+    float2* const sk = odd ? a.s1 : a.s0;         // s_k
+    const CgcgLd ld{rc, odd ? a.w1 : a.w0, odd ? a.s0 : a.s1, af, bf};
+    float ga = 0.f, de = 0.f;
+    auto epi = [&](int s, float2 wv, float2 u, const CgcgOp& o) {
+      const float2 pk = axpy2(bf, __ldcg(a.p0 + s), __ldcg(rc + s));
+      a.p0[s] = pk;
+      a.xs[s] = axpy2(af, pk, __ldcg(a.xs + s));
+      sk[s] = o.sk;
+      rn[s] = o.v;
+      wn[s] = wv;
+      ga = fmaf(o.v.x, o.v.x, fmaf(o.v.y, o.v.y, ga));
+      de = fmaf(u.x, u.x, fmaf(u.y, u.y, de));
+    };
+    stencil_mdagm<MU0>(g, a.km32, a.kd32, ld, a.Wt32, a.Wx32, epi);
+    CgcgScal e;
+    if (!grid_total2_then<BS>(ga, de, part(), a.bar, [&](double gn, double dn) {
+          CgcgScal o;
+          o.gam = gn;
+          o.beta = gn / gam;
+          o.alpha = gn / (dn - o.beta * gn / alpha);
+          o.need = since_ru + 1 >= a.ru_interval || gn < stop || gn < kRuDrop * rr_true || iter + 1 >= a.maxiter ||
+                   gn / rr0 > 1e10 || isnan(gn) || isnan(o.alpha);
+          return o;
+        }, e)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    iter += 1;
+    since_ru += 1;
+    const double alpha_prev = alpha, gam_prev = gam;
+    gam = e.gam;
+    alpha = e.alpha;
+    beta = e.beta;
+    rr = e.gam;
+    if (!e.need) continue;
+    // reliable update: x += xs, xs = 0; r_{k+1} = b - M^dag M x in FP64; then w_{k+1} = A r_{k+1}
+    TG_SITES(s, g.V) {
+      const float2 d = __ldcg(a.xs + s);
+      double2 xv = __ldcg(a.x + s);
+      xv.x += (double)d.x;
+      xv.y += (double)d.y;
+      a.x[s] = xv;
+      a.xs[s] = make_float2(0.f, 0.f);
+    }
+    if (!grid_barrier(a.bar)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    auto ld_x = [&](int i) { return __ldcg(a.x + i); };
+    auto epi_x = [&](int s, double2 o, double2) { a.tmp[s] = o; };
+    stencil_ld<double, 0, MU0>(g, a.km, ld_x, a.Wt, a.Wx, epi_x);
+    if (!grid_barrier(a.bar)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    double vt = 0;
+    auto ld_t = [&](int i) { return __ldcg(a.tmp + i); };
+    auto epi_t = [&](int s, double2 ap, double2) {
+      const double2 bb = a.b[s];
+      const double2 rv = make_double2(bb.x - ap.x, bb.y - ap.y);
+      rn[s] = make_float2((float)rv.x, (float)rv.y);
+      vt = fma(rv.x, rv.x, vt);
+      vt = fma(rv.y, rv.y, vt);
+    };
+    stencil_ld<double, 1, MU0>(g, a.kd, ld_t, a.Wt, a.Wx, epi_t);
+    double rt;
+    if (!grid_total<BS>(vt, part(), a.bar, rt)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    const bool restart = rt > kRuRestart * rr;  // the recursive residual was far too optimistic
+    rr_true = rt;
+    rr = rt;
+    since_ru = 0;
+    n_ru += 1;
+    if (isnan(rt)) status = TG_E_NAN;
+    else if (rt < stop) status = TG_OK;
+    else if (rt / rr0 > 1e10) status = TG_E_DIVERGED;
+    else if (iter >= a.maxiter) status = TG_E_NOCONV;
+    if (status >= 0) break;
+    // w_{k+1} = A r_{k+1} for the replaced r; alpha, beta from its gamma, delta
+    if (!first_w(rn, wn)) {
+      status = TG_E_TIMEOUT;
+      break;
+    }
+    if (restart) {  // p and s restart from r and w
+      beta = 0;
+      alpha = gam / del;
+    } else {
+      beta = gam / gam_prev;
+      alpha = gam / (del - beta * gam / alpha_prev);
+    }
   }
   pcg_report(a.st, a.log, a.log_index, rr, rr0, stop, iter, n_ru, status);
 }
@@ -471,6 +728,12 @@ cudaError_t barrier_check(cudaStream_t s, unsigned* count, unsigned phantom, lon
 cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a) {
   if (mu0) return pcg_launch(a.g, k_pcgmx<512, true>, k_pcgmx<256, true>, s, a);
   return pcg_launch(a.g, k_pcgmx<512, false>, k_pcgmx<256, false>, s, a);
+}
+
+cudaError_t pcgcg(cudaStream_t s, bool mu0, PcgMxArgs a) {
+  if (!a.g.march) return cudaErrorInvalidValue;
+  if (mu0) return pcg_launch(a.g, k_pcgcg<512, true>, k_pcgcg<256, true>, s, a);
+  return pcg_launch(a.g, k_pcgcg<512, false>, k_pcgcg<256, false>, s, a);
 }
 
 }  // namespace tg
