@@ -486,6 +486,7 @@ def run_ours(args, ws, rank, local):
     L2048.set_gauge(np.random.default_rng(2048).normal(0, 0.5, (n2, n2, 2)))
     t2_M = L2048.time_apply(20, False, tg.native.PREC_FP64)
     t2_M32 = L2048.time_apply(20, False, tg.native.PREC_MIXED)
+    cg_2048 = cg_solve_rates(tg, torch, L2048, n2, dev)
     L2048.close()
     dslash_2048 = {"fp64_ms": t2_M, "fp64_gbs": 64 * n2 * n2 / (t2_M * 1e-3) / 1e9,
                    "fp32_ms": t2_M32, "fp32_gbs": 32 * n2 * n2 / (t2_M32 * 1e-3) / 1e9}
@@ -554,6 +555,7 @@ def run_ours(args, ws, rank, local):
                    "fp32_gbs": dslash32_gbs, "fp32_ms": t_M32, "bytes_per_site_fp64": 64, "bytes_per_site_fp32": 32,
                    "at_2048": dict(dslash_2048, fp64_frac=dslash_2048["fp64_gbs"] / hbm,
                                    fp32_frac=dslash_2048["fp32_gbs"] / hbm)},
+        "cg_2048": cg_2048,
         "mixed": {"value": mixed_value, "unit": "trajectories/s", "speedup_vs_fp64": mixed_value / value,
                   "cg_iterations_per_traj": statistics.mean(r.cg_iterations for r in res_mx),
                   "reliable_updates_per_traj": statistics.mean(r.reliable_updates for r in res_mx),
@@ -569,6 +571,49 @@ def run_ours(args, ws, rank, local):
         cs = cpu_sample(iters / args.steps)
         line["cpu_baseline"] = {k: cs[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))
+
+
+# Algorithmic bytes per site of one FP32 CG iteration of the single-reduction
+# solver that 2048^2 runs: the elementwise update reads r, w, s, p, x and
+# writes s, p, x, r (72); the fused M^dag M pass reads r and the two links and
+# writes w (32).
+CG32_BYTES_PER_SITE = 104
+
+
+def cg_solve_rates(tg, torch, L, n, dev):
+    """One solve of M^dag M x = b to 1e-10 on the 2048^2 workload (m 0.02, g 0.8,
+    A ~ N(0, 0.5^2); FP32 with FP64 reliable updates every 50 iterations, and
+    FP64), device-resident, CUDA events on the lattice's stream, the second of
+    two solves: iterations, ms per iteration (the reliable updates included)
+    and, for the FP32 iteration, the HBM fraction at its algorithmic bytes."""
+    import ctypes as C
+    b = torch.from_numpy(np.random.default_rng(4096).normal(size=(n, n, 2))).to(dev)
+    x = torch.empty_like(b)
+    stream = torch.cuda.ExternalStream(L.lib.tg_stream(L.h), device=dev)
+    out = {}
+    for name, prec in (("fp64", tg.native.PREC_FP64), ("mixed", tg.native.PREC_MIXED)):
+        cp = tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=prec, ru_interval=50)
+        res = tg.native.CgResult()
+        for _ in range(2):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tg.native.check(L.lib.tg_cg_dev(L.h, C.byref(cp), C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()),
+                                            C.byref(res)))
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"iterations": res.iterations, "reliable_updates": res.reliable_updates, "ms": ms,
+                     "us_per_iteration": 1000 * ms / res.iterations, "status": res.status}
+    hbm, kind = peaks()
+    mx = out["mixed"]
+    mx["bytes_per_site"] = CG32_BYTES_PER_SITE
+    mx["achieved_gbs"] = CG32_BYTES_PER_SITE * n * n / (mx["us_per_iteration"] * 1e-6) / 1e9
+    mx["hbm_frac"] = mx["achieved_gbs"] / hbm
+    mx["peak_source"] = kind
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["ms"] / mx["ms"]
+    out["workload"] = "2048x2048, m 0.02, g 0.8, A ~ N(0, 0.5^2), CG to 1e-10, reliable updates every 50"
+    return out
 
 
 STABLE_TAU = 0.05

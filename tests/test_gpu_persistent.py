@@ -153,26 +153,28 @@ def test_grid_barrier_gives_up_and_device_stays_usable(tg):
 
 
 @pytest.mark.parametrize("nt,nx,mu,m,tol", [(64, 64, 0.0, 0.1, 1e-10), (32, 96, 0.3, 0.2, 1e-12), (256, 256, 0.0, 0.05, 1e-10),
-                                            (4, 32, 0.0, 0.3, 1e-10), (1024, 1024, 0.0, 0.05, 1e-10)])
+                                            (4, 32, 0.0, 0.3, 1e-10), (1024, 1024, 0.0, 0.05, 1e-10),
+                                            (2048, 2048, 0.0, 0.02, 1e-10)])
 def test_single_reduction_mixed_cg(tg, oracle_lib, monkeypatch, nt, nx, mu, m, tol):
-    """The mixed persistent solve on column-march lattices runs as the
-    single-reduction CG (one grid sum and one fused M^dag M pass per
-    iteration).  Against the two-sum form (TG_MIXED_CG=twosum) on the same
-    system: the same status, iteration counts within 2%, solutions within the
-    tolerance's reach, and the true residual |b - M^dag M x| / |b| (oracle, FP64)
-    below the target."""
+    """The single-reduction mixed CG on column-march lattices (one grid sum and
+    one fused M^dag M pass per iteration, after an elementwise update;
+    TG_MIXED_CG=onesum; the default above 1.5 times the L2) against the two-sum
+    form on the same system: the same status, iteration counts within 2%,
+    solutions within the tolerance's reach, and the true residual
+    |b - M^dag M x| / |b| (oracle, FP64) below the target."""
+    form = "onesum"
     rng = np.random.default_rng(nt + 7 * nx)
     A = rng.normal(0, 0.3, (nt, nx, 2))
     b = cplx(rng, (nt, nx))
     cp = tg.cg_params(rel_tol=tol, abs_tol2=0, precision=tg.native.PREC_MIXED, ru_interval=50, solver=PERSISTENT)
     out = {}
-    for form in ("twosum", "onesum"):
-        monkeypatch.setenv("TG_MIXED_CG", form)
+    for f in ("twosum", form):
+        monkeypatch.setenv("TG_MIXED_CG", f)
         L = tg.Lattice(nt, nx, m, 0.5, mu, -1, 1)
         L.set_gauge(A)
-        out[form] = L.fmdm_invert_cg(b, cp)
+        out[f] = L.fmdm_invert_cg(b, cp)
         L.close()
-    (x2, r2), (x1, r1) = out["twosum"], out["onesum"]
+    (x2, r2), (x1, r1) = out["twosum"], out[form]
     assert r1.status == r2.status == 0
     assert abs(r1.iterations - r2.iterations) <= max(2, r2.iterations // 50), (r1.iterations, r2.iterations)
     assert r1.reliable_updates >= 1
@@ -180,3 +182,19 @@ def test_single_reduction_mixed_cg(tg, oracle_lib, monkeypatch, nt, nx, mu, m, t
     o = oracle_lib.Oracle(nt, nx, m, 0.5, mu, -1, 1)
     true = np.linalg.norm(b - o.Mdag(A, o.M(A, x1))) / np.linalg.norm(b)
     assert true < 1.5 * tol, true
+
+
+def test_single_reduction_trajectories_match_reference(tg, monkeypatch):
+    """Whole trajectories with the single-reduction mixed CG on a column-march
+    reference fixture: dH within 1e-9 of the reference's, same decisions."""
+    monkeypatch.setenv("TG_MIXED_CG", "onesum")
+    d = golden("march_32x64_mu_px")
+    hp = tg.hmc_params(nsteps=int(d["traj_nsteps"]), tau=1.0, npf=1, stochastic_term=True, rng=tg.native.RNG_MT,
+                       cg=tg.cg_params(rel_tol=1e-13, abs_tol2=0, precision=tg.native.PREC_MIXED, ru_interval=50,
+                                       solver=PERSISTENT))
+    L, res = _replay(tg, d, hp)
+    for k, (r, want) in enumerate(zip(res, d["traj_stats"])):
+        assert r.status == 0
+        assert abs(r.dH - want[0]) <= 1e-9, (k, r.dH, want[0])
+        assert r.accepted == int(want[9])
+    assert np.abs(L.get_gauge() - d["traj_A"][-1]).max() <= 1e-9

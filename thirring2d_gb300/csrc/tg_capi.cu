@@ -136,6 +136,7 @@ struct tg_lattice {
   bool mt_seeded = false;
   std::map<std::string, GraphEntry> graphs;
   std::vector<cudaEvent_t> ev;
+  double l2_bytes = 0;  // the device's L2 size
 };
 
 namespace {
@@ -285,15 +286,20 @@ bool use_persistent(const tg_cg_params& cp) {
   return kDefaultPersistent;
 }
 
-// The mixed persistent solve runs the two-sum CG (k_pcgmx) by default;
-// TG_MIXED_CG=onesum selects, on column-march lattices, the single-reduction
-// CG (k_pcgcg: one grid sum and one fused M^dag M pass per iteration), which
-// measured slower on GB300 (1024^2: 27.7 against 21.8 us per iteration; 2048^2:
-// 122 against 103 us): its fused pass is latency-bound.
+// The mixed persistent solve on column-march lattices whose FP32 CG working set
+// (r, w, s, p, x and the two links: 56 B per site) is more than 1.5 times the
+// L2 runs the single-reduction CG (k_pcgcg: one grid sum and one fused
+// M^dag M pass per iteration); smaller lattices, whose vectors stay in L2 and
+// where the fused pass's halo recomputation costs more latency than the second
+// sum, run the two-sum CG (k_pcgmx).  Measured on GB300 (us per iteration,
+// fused / two-sum): 1024^2 30.3 / 21.7, 1536^2 58.1 / 58.6, 2048^2 93.8 / 102.5.
+// TG_MIXED_CG=twosum|onesum overrides.
 bool use_single_reduction(const tg_lattice* L) {
   if (!L->g.march) return false;
   const char* e = getenv("TG_MIXED_CG");
-  return e && strcmp(e, "onesum") == 0;
+  if (e && strcmp(e, "twosum") == 0) return false;
+  if (e && strcmp(e, "onesum") == 0) return true;
+  return 56.0 * (double)L->V > 1.5 * (double)L->l2_bytes;
 }
 
 // The whole solve as one cooperative launch (tg_pcg.cu); the barrier's
@@ -332,11 +338,8 @@ int enqueue_pcg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const dou
     a.maxiter = cp.maxiter;
     a.ru_interval = cp.ru_interval;
     if (use_single_reduction(L)) {
-      a.r1 = L->wmx.ps[1];
       a.w0 = L->wmx.Mps;
-      a.w1 = L->wmx.xtra[0];
-      a.s0 = L->wmx.xtra[1];
-      a.s1 = L->wmx.xtra[2];
+      a.s0 = L->wmx.ss;
       e = pcgcg(s, L->P.mu == 0.0, a);
     } else {
       e = pcgmx(s, L->P.mu == 0.0, a);
@@ -763,8 +766,10 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
   L->g.V = (int)V;
   L->g.inv_nx = 1.0f / (float)p->nx;
   {
-    int sms = 0;
+    int sms = 0, l2 = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess || sms <= 0) sms = 1;
+    if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, p->device) != cudaSuccess || l2 <= 0) l2 = 128 << 20;
+    L->l2_bytes = (double)l2;
     // 8 resident 256-thread blocks per SM at <= 32 registers per thread
     int cap = 8 * sms;
     L->g.grid = nblocks((int)V) < cap ? nblocks((int)V) : cap;
@@ -786,7 +791,7 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
   for (auto pp : d2)
     if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
   float2** f2[] = {&L->Wt32, &L->Wx32, &L->wmx.xs, &L->wmx.rs, &L->wmx.ps[0], &L->wmx.ps[1], &L->wmx.Mps,
-                   &L->wmx.xtra[0], &L->wmx.xtra[1], &L->wmx.xtra[2]};
+                   &L->wmx.ss};
   for (auto pp : f2)
     if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
   if ((rc = dmalloc(&L->st, 1)) != TG_OK || (rc = dmalloc(&L->log, kMaxLog)) != TG_OK ||
@@ -827,7 +832,7 @@ int tg_destroy(tg_lattice* L) {
   for (auto e : L->ev) cudaEventDestroy(e);
   void* dev[] = {L->A, L->Anew, L->Wt, L->Wx, L->Wt1, L->Wx1, L->mom, L->noise, L->chi, L->Mchi, L->vin, L->vout, L->w64.r,
                  L->w64.p[0], L->w64.p[1], L->w64.Mp, L->wmx.tmp64, L->Wt32, L->Wx32, L->wmx.xs, L->wmx.rs,
-                 L->wmx.ps[0], L->wmx.ps[1], L->wmx.Mps, L->wmx.xtra[0], L->wmx.xtra[1], L->wmx.xtra[2],
+                 L->wmx.ps[0], L->wmx.ps[1], L->wmx.Mps, L->wmx.ss,
                  L->st, L->log, L->ts, L->red.partials, L->red.counter, L->bar, L->pcg_part, L->eta, L->phi, L->unif, L->mask,
                  L->rv[0], L->rv[1], L->rv[2], L->rv[3], L->rv[4], L->rv[5]};
   for (void* d : dev)

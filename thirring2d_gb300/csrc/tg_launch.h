@@ -20,7 +20,7 @@ struct CgBufs64 {          // FP64 CG work vectors (p alternates between two buf
 struct CgBufsMixed {       // FP32 CG work vectors + FP64 accumulators
   float2 *xs, *rs, *ps[2], *Mps;
   double2* tmp64;          // M x for the reliable update
-  float2* xtra[3];         // single-reduction CG: its second r, second w and two s buffers with ps[1], Mps
+  float2* ss;              // single-reduction CG: s (its w is Mps, p ps[0], r rs)
 };
 
 struct Red {               // reduction scratch
@@ -148,8 +148,8 @@ struct PcgMxArgs {
   const double2* b;
   double2 *x, *tmp;
   float2 *xs, *r, *p0, *p1, *Mp;
-  // single-reduction CG (k_pcgcg): r alternates r/r1, w w0/w1, s s0/s1; p0 is p
-  float2 *r1, *w0, *w1, *s0, *s1;
+  // single-reduction CG (k_pcgcg): w and s; p0 is p, r is r
+  float2 *w0, *s0;
   CgState* st;
   CgLog* log;
   int log_index;
@@ -161,8 +161,9 @@ struct PcgMxArgs {
 
 cudaError_t pcg64(cudaStream_t s, bool mu0, Pcg64Args a);
 cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a);
-// the mixed solve as a single-reduction CG whose pass applies M^dag M in one
-// column march (lattices with g.march only); same arguments and results
+// the mixed solve as a single-reduction CG (lattices with g.march only; same
+// arguments and results): per iteration an elementwise update and one pass of
+// the fused M^dag M march (k_pcgcg)
 cudaError_t pcgcg(cudaStream_t s, bool mu0, PcgMxArgs a);
 // one grid barrier (4 blocks, cooperative) that also waits for `phantom` absent
 // blocks, giving up after `limit` polls: *status = TG_OK or TG_E_TIMEOUT

@@ -390,49 +390,71 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
 //   gamma = (r_{k+1}, r_{k+1}),  delta = (r_{k+1}, A r_{k+1}) = |M r_{k+1}|^2,
 //   beta_{k+1} = gamma / gamma_k,  alpha_{k+1} = gamma / (delta - beta_{k+1} gamma / alpha_k),
 // so one grid sum (gamma and delta together) per iteration instead of two.
-// Each iteration is one pass of the fused M^dag M march (tg_fused.cuh): the
-// loader forms s_k and r_{k+1} where it reads, at every site including the
-// halo, and the epilogue stores r_{k+1}, s_k, w_{k+1}, p_k and x_{k+1}.  r, s
-// and w alternate between two buffers (halo sites of other warps are still
-// read while a pass writes); p and x are only read where they are written.
+// An iteration runs in two phases:
+//   A  the vector updates (s, p, x, r in place), site by site: no neighbours,
+//      every load of a thread's sites issued before the first store;
+//   B  after a grid barrier, w = A r in one pass of the fused M^dag M march
+//      (tg_fused.cuh), which also forms the partials of gamma and delta.
 // Column-march lattices only (nx a multiple of 32, nt of kMarchT).
 // ---------------------------------------------------------------------------
-struct CgcgOp {
-  float2 v, sk;  // r_{k+1}, s_k at one site (the epilogue reads r_k again: registers)
-};
-__device__ __forceinline__ float2 axpy2(float a, float2 x, float2 y) {
-  return make_float2(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y));
-}
-struct CgcgLd {  // r_{k+1} = r_k - alpha_k (w_k + beta_k s_{k-1}) on the fly
-  using Op = CgcgOp;
-  const float2 *r, *w, *sp;
-  float al, be;
-  __device__ __forceinline__ Op own(int i) const {
-    const float2 rv = __ldcg(r + i), wv = __ldcg(w + i), sv = __ldcg(sp + i);
-    const float2 sk = axpy2(be, sv, wv);
-    return Op{axpy2(-al, sk, rv), sk};
-  }
-  __device__ __forceinline__ float2 val(int i) const { return own(i).v; }
-};
 struct PlainOp {
   float2 v;
 };
-struct PlainLd {  // the vector itself (the first w = A r, and after a reliable update)
+struct PlainLd {  // the fused march's operand: r itself
   using Op = PlainOp;
   const float2* r;
   __device__ __forceinline__ Op own(int i) const { return Op{__ldcg(r + i)}; }
   __device__ __forceinline__ float2 val(int i) const { return __ldcg(r + i); }
 };
 
-// The grid total of a pair of partials (gamma, delta): FP32 within a block, FP64
-// across blocks in index order, handed to f in thread 0 of every block.
-template <int BS, class F>
-__device__ __forceinline__ bool grid_total2_then(float va, float vb, double* part, const GridBar& bar, F f,
-                                                 decltype(f(0.0, 0.0))& out) {
-  using S = decltype(f(0.0, 0.0));
+__device__ __forceinline__ float2 axpy2(float a, float2 x, float2 y) {
+  return make_float2(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y));
+}
+__device__ __forceinline__ float4 axpy4(float a, float4 x, float4 y) {
+  return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+}
+
+// Phase A over two sites per float4, two float4 per thread in flight.
+__device__ __forceinline__ void cgcg_update(const Geo& g, float4* __restrict__ r, const float4* __restrict__ w,
+                                            float4* __restrict__ s, float4* __restrict__ p, float4* __restrict__ xs,
+                                            float al, float be) {
+  constexpr int U = 2;
+  const int n4 = g.V >> 1;  // V is even on column-march lattices
+  const int stride = gridDim.x * blockDim.x;
+  for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n4; i0 += U * stride) {
+    float4 rv[U], wv[U], sv[U], pv[U], xv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int i = i0 + u * stride;
+      if (i < n4) {
+        rv[u] = __ldcg(r + i);
+        wv[u] = __ldcg(w + i);
+        sv[u] = __ldcg(s + i);
+        pv[u] = __ldcg(p + i);
+        xv[u] = __ldcg(xs + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int i = i0 + u * stride;
+      if (i < n4) {
+        const float4 sk = axpy4(be, sv[u], wv[u]);
+        const float4 pk = axpy4(be, pv[u], rv[u]);
+        s[i] = sk;
+        p[i] = pk;
+        xs[i] = axpy4(al, pk, xv[u]);
+        r[i] = axpy4(-al, sk, rv[u]);
+      }
+    }
+  }
+}
+
+// Block sums of a pair of partials (gamma, delta) in FP32, written to part as
+// FP64 (grid_publish2); after the grid barrier that follows, every block adds
+// all blocks' pairs in index order (grid_read2).
+template <int BS>
+__device__ __forceinline__ void grid_publish2(float va, float vb, double* part) {
   __shared__ float sha[BS / 32], shb[BS / 32];
-  __shared__ double sda[BS / 32], sdb[BS / 32];
-  __shared__ S s_out;
   va = warp_sum(va);
   vb = warp_sum(vb);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -450,7 +472,12 @@ __device__ __forceinline__ bool grid_total2_then(float va, float vb, double* par
       part[2 * blockIdx.x + 1] = (double)b;
     }
   }
-  if (!grid_barrier(bar)) return false;
+}
+template <int BS>
+__device__ __forceinline__ double2 grid_read2(const double* part) {
+  __shared__ double sda[BS / 32], sdb[BS / 32];
+  __shared__ double2 s_out;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double a = 0, b = 0;
   for (int i = threadIdx.x; i < (int)gridDim.x; i += BS) {
     a += __ldcg(part + 2 * i);
@@ -469,17 +496,69 @@ __device__ __forceinline__ bool grid_total2_then(float va, float vb, double* par
       ta += sda[k];
       tb += sdb[k];
     }
-    s_out = f(ta, tb);
+    s_out = make_double2(ta, tb);
   }
   __syncthreads();
-  out = s_out;
-  return true;
+  return s_out;
 }
 
-struct CgcgScal {
-  double gam, alpha, beta;
-  int need;  // a reliable update is due
-};
+// The FP64 reliable update shared by the single-reduction kernels:
+// x += xs, xs = 0; r = (float)(b - M^dag M x) with |b - M^dag M x|^2 summed
+// into rt.  False if a grid barrier gave up.
+template <int BS, bool MU0, class Part>
+__device__ __forceinline__ bool cgcg_reliable(const PcgMxArgs& a, float2* r, Part& part, double& rt) {
+  const Geo& g = a.g;
+  TG_SITES(s, g.V) {
+    const float2 d = __ldcg(a.xs + s);
+    double2 xv = __ldcg(a.x + s);
+    xv.x += (double)d.x;
+    xv.y += (double)d.y;
+    a.x[s] = xv;
+    a.xs[s] = make_float2(0.f, 0.f);
+  }
+  if (!grid_barrier(a.bar)) return false;
+  auto ld_x = [&](int i) { return __ldcg(a.x + i); };
+  auto epi_x = [&](int s, double2 o, double2) { a.tmp[s] = o; };
+  stencil_ld<double, 0, MU0>(g, a.km, ld_x, a.Wt, a.Wx, epi_x);
+  if (!grid_barrier(a.bar)) return false;
+  double vt = 0;
+  auto ld_t = [&](int i) { return __ldcg(a.tmp + i); };
+  auto epi_t = [&](int s, double2 ap, double2) {
+    const double2 bb = a.b[s];
+    const double2 rv = make_double2(bb.x - ap.x, bb.y - ap.y);
+    r[s] = make_float2((float)rv.x, (float)rv.y);
+    vt = fma(rv.x, rv.x, vt);
+    vt = fma(rv.y, rv.y, vt);
+  };
+  stencil_ld<double, 1, MU0>(g, a.kd, ld_t, a.Wt, a.Wx, epi_t);
+  return grid_total<BS>(vt, part(), a.bar, rt);
+}
+
+// x = 0, r_0 = b, p_{-1} = s_{-1} = 0 and |b|^2 (shared set-up)
+template <int BS, class Part>
+__device__ __forceinline__ bool cgcg_start(const PcgMxArgs& a, float2* r, float2* p, float2* sv, Part& part,
+                                           double& rr) {
+  double v = 0;
+  TG_SITES(s, a.g.V) {
+    const double2 bb = a.b[s];
+    a.x[s] = make_double2(0.0, 0.0);
+    a.xs[s] = make_float2(0.f, 0.f);
+    r[s] = make_float2((float)bb.x, (float)bb.y);
+    p[s] = make_float2(0.f, 0.f);
+    sv[s] = make_float2(0.f, 0.f);
+    v = fma(bb.x, bb.x, v);
+    v = fma(bb.y, bb.y, v);
+  }
+  return grid_total<BS>(v, part(), a.bar, rr);
+}
+
+__device__ __forceinline__ int ru_status(double rt, double stop, double rr0, int iter, int maxiter) {
+  if (isnan(rt)) return TG_E_NAN;
+  if (rt < stop) return TG_OK;
+  if (rt / rr0 > 1e10) return TG_E_DIVERGED;
+  if (iter >= maxiter) return TG_E_NOCONV;
+  return -1;
+}
 
 template <int BS, bool MU0>
 __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgcg(PcgMxArgs a) {
@@ -490,20 +569,10 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgcg(PcgMxArgs a) {
   // writes the other array, never one that a slower block is still reading.
   int nsum = 0;
   auto part = [&]() { return a.part + 2 * gridDim.x * ((nsum++) & 1); };
-  double v = 0;
-  TG_SITES(s, g.V) {  // x = 0, r_0 = b, p_{-1} = s_{-1} = 0
-    const double2 bb = a.b[s];
-    a.x[s] = make_double2(0.0, 0.0);
-    a.xs[s] = make_float2(0.f, 0.f);
-    a.r[s] = make_float2((float)bb.x, (float)bb.y);
-    a.p0[s] = make_float2(0.f, 0.f);
-    a.s1[s] = make_float2(0.f, 0.f);
-    v = fma(bb.x, bb.x, v);
-    v = fma(bb.y, bb.y, v);
-  }
+  float2 *const r = a.r, *const w = a.w0, *const sv = a.s0, *const p = a.p0;
   double rr = 0;
   int status = -1, iter = 0, n_ru = 0, since_ru = 0;
-  if (!grid_total<BS>(v, part(), a.bar, rr)) status = TG_E_TIMEOUT;
+  if (!cgcg_start<BS>(a, r, p, sv, part, rr)) status = TG_E_TIMEOUT;
   const double rr0 = rr;
   const double stop = stop_of(rr0, a.rel_tol, a.abs_tol2);
   double rr_true = rr;
@@ -511,9 +580,8 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgcg(PcgMxArgs a) {
     if (isnan(rr)) status = TG_E_NAN;
     else if (!(rr >= stop) || rr == 0.0) status = TG_OK;
   }
-  // w_0 = A r_0; gamma_0, delta_0
-  double gam = 0, del = 0, alpha = 0, beta = 0;
-  auto first_w = [&](float2* r, float2* w) -> bool {  // w = A r; gam, del = (r, r), (r, A r)
+  // phase B: w = A r and the totals of (r, r) and (r, A r)
+  auto apply_sum = [&](double2& gd) -> bool {
     float ga = 0.f, de = 0.f;
     const PlainLd ld{r};
     auto epi = [&](int s, float2 wv, float2 u, const PlainOp& o) {
@@ -522,90 +590,44 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgcg(PcgMxArgs a) {
       de = fmaf(u.x, u.x, fmaf(u.y, u.y, de));
     };
     stencil_mdagm<MU0>(g, a.km32, a.kd32, ld, a.Wt32, a.Wx32, epi);
-    double2 gd;
-    if (!grid_total2_then<BS>(ga, de, part(), a.bar, [](double x, double y) { return make_double2(x, y); }, gd))
-      return false;
-    gam = gd.x;
-    del = gd.y;
+    double* pp = part();
+    grid_publish2<BS>(ga, de, pp);
+    if (!grid_barrier(a.bar)) return false;
+    gd = grid_read2<BS>(pp);
     return true;
   };
+  double gam = 0, alpha = 0, beta = 0;
   if (status < 0) {
-    if (first_w(a.r, a.w0)) alpha = gam / del;
-    else status = TG_E_TIMEOUT;
+    double2 gd;
+    if (apply_sum(gd)) {
+      gam = gd.x;
+      alpha = gd.x / gd.y;
+    } else {
+      status = TG_E_TIMEOUT;
+    }
   }
   while (status < 0) {
-    const bool odd = iter & 1;
-    const float af = (float)alpha, bf = (float)beta;
-    const float2* const rc = odd ? a.r1 : a.r;   // r_k
-    float2* const rn = odd ? a.r : a.r1;          // r_{k+1}
-    float2* const wn = odd ? a.w0 : a.w1;         // w_{k+1}
-    float2* const sk = odd ? a.s1 : a.s0;         // s_k
-    const CgcgLd ld{rc, odd ? a.w1 : a.w0, odd ? a.s0 : a.s1, af, bf};
-    float ga = 0.f, de = 0.f;
-    auto epi = [&](int s, float2 wv, float2 u, const CgcgOp& o) {
-      const float2 pk = axpy2(bf, __ldcg(a.p0 + s), __ldcg(rc + s));
-      a.p0[s] = pk;
-      a.xs[s] = axpy2(af, pk, __ldcg(a.xs + s));
-      sk[s] = o.sk;
-      rn[s] = o.v;
-      wn[s] = wv;
-      ga = fmaf(o.v.x, o.v.x, fmaf(o.v.y, o.v.y, ga));
-      de = fmaf(u.x, u.x, fmaf(u.y, u.y, de));
-    };
-    stencil_mdagm<MU0>(g, a.km32, a.kd32, ld, a.Wt32, a.Wx32, epi);
-    CgcgScal e;
-    if (!grid_total2_then<BS>(ga, de, part(), a.bar, [&](double gn, double dn) {
-          CgcgScal o;
-          o.gam = gn;
-          o.beta = gn / gam;
-          o.alpha = gn / (dn - o.beta * gn / alpha);
-          o.need = since_ru + 1 >= a.ru_interval || gn < stop || gn < kRuDrop * rr_true || iter + 1 >= a.maxiter ||
-                   gn / rr0 > 1e10 || isnan(gn) || isnan(o.alpha);
-          return o;
-        }, e)) {
+    cgcg_update(g, reinterpret_cast<float4*>(r), reinterpret_cast<const float4*>(w), reinterpret_cast<float4*>(sv),
+                reinterpret_cast<float4*>(p), reinterpret_cast<float4*>(a.xs), (float)alpha, (float)beta);
+    double2 gd;
+    if (!grid_barrier(a.bar) || !apply_sum(gd)) {
       status = TG_E_TIMEOUT;
       break;
     }
+    const double gn = gd.x, dn = gd.y;
+    const bool need = since_ru + 1 >= a.ru_interval || gn < stop || gn < kRuDrop * rr_true ||
+                      iter + 1 >= a.maxiter || gn / rr0 > 1e10 || isnan(gn) || isnan(dn);
     iter += 1;
     since_ru += 1;
     const double alpha_prev = alpha, gam_prev = gam;
-    gam = e.gam;
-    alpha = e.alpha;
-    beta = e.beta;
-    rr = e.gam;
-    if (!e.need) continue;
-    // reliable update: x += xs, xs = 0; r_{k+1} = b - M^dag M x in FP64; then w_{k+1} = A r_{k+1}
-    TG_SITES(s, g.V) {
-      const float2 d = __ldcg(a.xs + s);
-      double2 xv = __ldcg(a.x + s);
-      xv.x += (double)d.x;
-      xv.y += (double)d.y;
-      a.x[s] = xv;
-      a.xs[s] = make_float2(0.f, 0.f);
-    }
-    if (!grid_barrier(a.bar)) {
-      status = TG_E_TIMEOUT;
-      break;
-    }
-    auto ld_x = [&](int i) { return __ldcg(a.x + i); };
-    auto epi_x = [&](int s, double2 o, double2) { a.tmp[s] = o; };
-    stencil_ld<double, 0, MU0>(g, a.km, ld_x, a.Wt, a.Wx, epi_x);
-    if (!grid_barrier(a.bar)) {
-      status = TG_E_TIMEOUT;
-      break;
-    }
-    double vt = 0;
-    auto ld_t = [&](int i) { return __ldcg(a.tmp + i); };
-    auto epi_t = [&](int s, double2 ap, double2) {
-      const double2 bb = a.b[s];
-      const double2 rv = make_double2(bb.x - ap.x, bb.y - ap.y);
-      rn[s] = make_float2((float)rv.x, (float)rv.y);
-      vt = fma(rv.x, rv.x, vt);
-      vt = fma(rv.y, rv.y, vt);
-    };
-    stencil_ld<double, 1, MU0>(g, a.kd, ld_t, a.Wt, a.Wx, epi_t);
+    beta = gn / gam;
+    alpha = gn / (dn - beta * gn / alpha);
+    gam = gn;
+    rr = gn;
+    if (!need) continue;
+    // reliable update, then w = A r for the replaced r
     double rt;
-    if (!grid_total<BS>(vt, part(), a.bar, rt)) {
+    if (!cgcg_reliable<BS, MU0>(a, r, part, rt)) {
       status = TG_E_TIMEOUT;
       break;
     }
@@ -614,23 +636,20 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgcg(PcgMxArgs a) {
     rr = rt;
     since_ru = 0;
     n_ru += 1;
-    if (isnan(rt)) status = TG_E_NAN;
-    else if (rt < stop) status = TG_OK;
-    else if (rt / rr0 > 1e10) status = TG_E_DIVERGED;
-    else if (iter >= a.maxiter) status = TG_E_NOCONV;
+    status = ru_status(rt, stop, rr0, iter, a.maxiter);
     if (status >= 0) break;
-    // w_{k+1} = A r_{k+1} for the replaced r; alpha, beta from its gamma, delta
-    if (!first_w(rn, wn)) {
+    if (!apply_sum(gd)) {
       status = TG_E_TIMEOUT;
       break;
     }
     if (restart) {  // p and s restart from r and w
       beta = 0;
-      alpha = gam / del;
+      alpha = gd.x / gd.y;
     } else {
-      beta = gam / gam_prev;
-      alpha = gam / (del - beta * gam / alpha_prev);
+      beta = gd.x / gam_prev;
+      alpha = gd.x / (gd.y - beta * gd.x / alpha_prev);
     }
+    gam = gd.x;
   }
   pcg_report(a.st, a.log, a.log_index, rr, rr0, stop, iter, n_ru, status);
 }
