@@ -51,6 +51,10 @@ __device__ __forceinline__ unsigned& barrier_epoch() {
 // polls a block gives up and returns false.
 __device__ __forceinline__ bool grid_barrier_n(const GridBar& b, unsigned nblocks, long long limit) {
   __shared__ int s_ok;
+  if (nblocks == 1) {  // a one-block grid (small lattices): the block barrier orders its global writes
+    __syncthreads();
+    return true;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned target = (barrier_epoch() += 1) * nblocks;
