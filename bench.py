@@ -678,7 +678,9 @@ def run_c1(tg, torch, dev, ntraj=200, nchains=512, batch_steps=5):
     out = {"config": "16x16, t antiperiodic, x periodic, m 0.1, g 0.5, mu 0, A ~ N(0, 0.1^2), 10 leapfrog steps, "
                      "tau 1, one pseudofermion", "single_chain": {}}
     for label, cp in (("fp64_cg_abs_1e-30", tg.cg_params()),
-                      ("fp64_cg_rel_1e-12", tg.cg_params(rel_tol=1e-12, abs_tol2=0.0))):
+                      ("fp64_cg_rel_1e-12", tg.cg_params(rel_tol=1e-12, abs_tol2=0.0)),
+                      ("mixed_cg_rel_1e-12", tg.cg_params(rel_tol=1e-12, abs_tol2=0.0, precision=tg.native.PREC_MIXED,
+                                                          ru_interval=50))):
         L = tg.Lattice(C1["nt"], C1["nx"], C1["m"], C1["g"], C1["mu"], C1["bc_t"], C1["bc_x"], device=dev.index)
         L.set_gauge(fields[0])
         L.seed_mersenne(1000, 543210)
@@ -693,6 +695,20 @@ def run_c1(tg, torch, dev, ntraj=200, nchains=512, batch_steps=5):
         out["single_chain"][label] = {"value": ntraj / dt, "unit": "trajectories/s", "trajectories": ntraj,
                                       "cg_iterations_per_traj": statistics.mean(r.cg_iterations for r in res),
                                       "acceptance": statistics.mean(r.accepted for r in res)}
+    # one chain alone on the batched kernel (Philox fields; the autotuner may
+    # spread it over a cluster of SMs)
+    one = {}
+    for name, prec in (("fp64", tg.native.PREC_FP64), ("mixed", tg.native.PREC_MIXED)):
+        B = tg.Batch(chains[:1])
+        B.set_gauge(0, fields[0])
+        cg = tg.cg_params(rel_tol=1e-12, abs_tol2=0.0, precision=prec, ru_interval=50)
+        block, _ = B.autotune(tg.batch_params(nsteps=C1["nsteps"], cg=cg))
+        bp = tg.batch_params(nsteps=C1["nsteps"], cg=cg, block=block)
+        B.trajectory(bp)
+        ms = sum(B.trajectory(bp)[0].cg_ms for _ in range(20))
+        B.close()
+        one[name] = {"value": 20 / (ms / 1e3), "unit": "trajectories/s", "cg_rel_tol": 1e-12, "kernel_instance": block}
+    out["single_chain"]["batched_kernel"] = one
     batch = {"chains": nchains}
     for name, prec in (("fp64", tg.native.PREC_FP64), ("mixed", tg.native.PREC_MIXED)):
         B = tg.Batch(chains)
@@ -711,6 +727,7 @@ def run_c1(tg, torch, dev, ntraj=200, nchains=512, batch_steps=5):
     ref = out["reference_host"]["value"]
     out["speedup_vs_reference_host"] = {
         "single_chain_fp64_same_cg_stop": out["single_chain"]["fp64_cg_abs_1e-30"]["value"] / ref,
+        "single_chain_mixed": out["single_chain"]["mixed_cg_rel_1e-12"]["value"] / ref,
         "batch_fp64": batch["fp64"]["value"] / ref, "batch_mixed": batch["mixed"]["value"] / ref}
     return out
 
