@@ -159,7 +159,7 @@ def replica_seed(rank: int) -> int:
 # ---------------------------------------------------------------------------
 # CPU reference timing (bounded sample)
 # ---------------------------------------------------------------------------
-def cpu_sample(iters_per_traj: float, repeats: int = 3):
+def cpu_sample(iters_per_traj: float, repeats: int = 3, count_source: str = "counted by the GPU arm of this run"):
     """Seconds per CG iteration and per operator apply of the reference hmc.c at
     1024^2 (oracle/_ref sample build: fmdm_invert_cg stops after 20 iterations),
     or of the oracle restatement where the reference build is absent, scaled
@@ -198,7 +198,7 @@ def cpu_sample(iters_per_traj: float, repeats: int = 3):
     t_traj = t_iter * iters_per_traj + t_apply * (W["nsteps"] + 3)
     sample = (f"{repeats} x {iters} iterations of fmdm_invert_cg + 1 fm_mul at {W['nt']}x{W['nx']} "
               f"({'reference hmc.c build' if kind == 'reference' else 'oracle restatement'}), "
-              f"scaled by {iters_per_traj:.0f} CG iterations (counted by the GPU arm of this run) and "
+              f"scaled by {iters_per_traj:.0f} CG iterations ({count_source}) and "
               f"{W['nsteps'] + 3} applies per trajectory")
     return dict(value=1.0 / t_traj, unit="trajectories/s", cores=1, kind=kind, sample=sample,
                 sec_per_cg_iter=t_iter, sec_per_apply=t_apply)
@@ -366,7 +366,7 @@ def run_reference(args, ws, rank):
     first_solve = host_iteration_count()
     iters_per_traj = first_solve * SOLVES_PER_TRAJ
     # the serial reference as it runs, one process on one core (for context)
-    single = cpu_sample(iters_per_traj, repeats=1)
+    single = cpu_sample(iters_per_traj, repeats=1, count_source="counted on the host, as below")
     # the whole host: one reference process per core, all at once; each step is
     # one such sample of `seconds` per process
     cores, seconds = host_cores(), 5.0

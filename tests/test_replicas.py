@@ -89,7 +89,8 @@ def test_reference_arm_reports_the_whole_host(capsys, monkeypatch):
     monkeypatch.setattr(bench, "cpu_host_sample", host_sample)
     monkeypatch.setattr(bench, "host_iteration_count", lambda: 300)
     monkeypatch.setattr(bench, "cpu_sample",
-                        lambda iters, repeats=1: dict(value=0.001, kind="reference", cores=1, sample="one core"))
+                        lambda iters, repeats=1, count_source="": dict(value=0.001, kind="reference", cores=1,
+                                                                       sample="one core"))
 
     class Args:
         steps, warmup, gpus = 3, 1, 1
