@@ -528,6 +528,8 @@ def run_ours(args, ws, rank, local):
         # the HBM fraction a CG iteration reaches when the FP64 pipe runs at its peak
         return (fp64_peak * 1e12 / CG_ITER_FP64_FLOPS_PER_SITE * CG_ITER_BYTES_PER_SITE / 1e9) / hbm_gbs
 
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    issue_tflops = 2 * 2 * sms * (clocks.get("sm_max_mhz") or 2070.0) * 1e6 / 1e12
     if rank != 0:
         return
     line = {
@@ -550,6 +552,8 @@ def run_ours(args, ws, rank, local):
                              "FP64 FMA rate; dslash.at_2048.fp32_frac is the HBM-bound FP32 stencil's"},
         "fp64_alu": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak, "peak_source": fp64_peak_kind,
                      "frac": fp64_achieved / fp64_peak, "flops_per_site": CG_ITER_FP64_FLOPS_PER_SITE,
+                     "issue_rate_tflops": issue_tflops, "frac_of_issue_rate": fp64_achieved / issue_tflops,
+                     "issue_rate_source": "2 DFMA per SM per clock x SMs x the sampled maximum SM clock",
                      "note": "the FP64 CG keeps the FP64 pipe busy most of the time (ncu); it is FP64-ALU-bound"},
         "dslash": {"fp64_gbs": dslash_gbs, "fp64_ms_M": t_M, "fp64_ms_Mdag": t_Md, "fp64_frac": dslash_gbs / hbm,
                    "fp32_gbs": dslash32_gbs, "fp32_ms": t_M32, "bytes_per_site_fp64": 64, "bytes_per_site_fp32": 32,

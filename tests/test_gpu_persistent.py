@@ -100,6 +100,35 @@ def test_persistent_edge_cases(tg, precision):
     assert res.status == 0
 
 
+def test_single_reduction_edge_cases(tg, monkeypatch):
+    """The single-reduction mixed CG (TG_MIXED_CG=onesum) on a column-march
+    lattice: b = 0 returns x = 0 at once (hmc.c:359-361), the iteration cap
+    reports TG_E_NOCONV with exactly that many iterations, a NaN in b reports
+    TG_E_NAN, a singular operator ends with a failure status, and the lattice
+    solves normally afterwards."""
+    monkeypatch.setenv("TG_MIXED_CG", "onesum")
+    rng = np.random.default_rng(19)
+    L = tg.Lattice(32, 32, 0.3, 0.5, 0.0, -1, 1)
+    L.set_gauge(rng.normal(0, 0.5, (32, 32, 2)))
+    cp = dict(solver=PERSISTENT, precision=tg.native.PREC_MIXED, ru_interval=50)
+    x, res = L.fmdm_invert_cg(np.zeros((32, 32), complex), tg.cg_params(**cp))
+    assert res.status == 0 and res.iterations == 0 and not x.any()
+    x, res = L.fmdm_invert_cg(cplx(rng, (32, 32)), tg.cg_params(maxiter=3, **cp))
+    assert res.status == tg.native.TG_E_NOCONV and res.iterations == 3
+    bad = cplx(rng, (32, 32))
+    bad[2, 3] = np.nan
+    x, res = L.fmdm_invert_cg(bad, tg.cg_params(**cp))
+    assert res.status == tg.native.TG_E_NAN
+    x, res = L.fmdm_invert_cg(cplx(rng, (32, 32)), tg.cg_params(rel_tol=1e-10, abs_tol2=0, **cp))
+    assert res.status == 0
+    S = tg.Lattice(32, 32, 0.0, 0.5, 0.0, 1, 1)   # m = 0, periodic, A = 0: exact zero modes
+    x, res = S.fmdm_invert_cg(cplx(rng, (32, 32)), tg.cg_params(rel_tol=1e-12, abs_tol2=0, maxiter=5000, **cp))
+    assert res.status in (tg.native.TG_E_DIVERGED, tg.native.TG_E_NAN, tg.native.TG_E_NOCONV)
+    S.set_couplings(0.3, 0.5, 0.0)
+    x, res = S.fmdm_invert_cg(cplx(rng, (32, 32)), tg.cg_params(rel_tol=1e-10, abs_tol2=0, **cp))
+    assert res.status == 0
+
+
 def _replay(tg, d, hp):
     L = make(tg, d)
     L.seed_mersenne(int(d["traj_seed"]), 543210)
