@@ -227,3 +227,20 @@ def test_single_reduction_trajectories_match_reference(tg, monkeypatch):
         assert abs(r.dH - want[0]) <= 1e-9, (k, r.dH, want[0])
         assert r.accepted == int(want[9])
     assert np.abs(L.get_gauge() - d["traj_A"][-1]).max() <= 1e-9
+
+
+def test_single_reduction_graph_equals_eager(tg, monkeypatch):
+    """The single-reduction mixed solve inside a trajectory captured as a CUDA
+    graph and launched eagerly: the same kernels on the same data, so bitwise
+    the same dH, decisions and field."""
+    monkeypatch.setenv("TG_MIXED_CG", "onesum")
+    d = golden("march_32x96_apx")
+    runs = []
+    for use_graph in (True, False):
+        hp = tg.hmc_params(nsteps=int(d["traj_nsteps"]), rng=tg.native.RNG_MT, use_graph=use_graph,
+                           cg=tg.cg_params(rel_tol=1e-12, abs_tol2=0, precision=tg.native.PREC_MIXED, ru_interval=50,
+                                           solver=PERSISTENT))
+        L, res = _replay(tg, d, hp)
+        runs.append(([r.dH for r in res], [r.accepted for r in res], L.get_gauge()))
+    assert runs[0][0] == runs[1][0] and runs[0][1] == runs[1][1]
+    assert np.array_equal(runs[0][2], runs[1][2])
