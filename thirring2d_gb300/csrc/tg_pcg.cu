@@ -4,7 +4,7 @@
 //
 // All blocks are co-resident (cooperative launch) and meet at a grid barrier
 // after each reduction.  Every block writes its partial sum, passes the
-// barrier, and then adds all partials in index order itself, so every block
+// barrier, and then adds all partials in a fixed order itself, so every block
 // holds the same bitwise total and takes the same branch: control flow stays
 // uniform across the grid without a broadcast.  Two partial arrays alternate,
 // so a block that races ahead never overwrites partials another block is
@@ -96,25 +96,54 @@ __global__ void k_barrier_check(GridBar b, unsigned phantom, long long limit, in
   if (blockIdx.x == 0 && threadIdx.x == 0) *status = ok ? TG_OK : TG_E_TIMEOUT;
 }
 
+// Warp 0's read of the blocks' partials after a grid barrier: NP values per
+// block, part[NP * i + k].  Each lane adds the blocks lane, lane + 32, ... in
+// index order, with the loads of up to 256 blocks in flight at once (a loop
+// would wait one L2 round trip per block), then a fixed shuffle tree; the
+// totals are valid in lane 0.  Measured 0.17 us faster per sum than a read by
+// all threads with a block-wide tree.
+template <int NP>
+__device__ __forceinline__ void warp_read_partials(const double* part, double (&tot)[NP]) {
+  const int lane = threadIdx.x & 31, nb = (int)gridDim.x;
+#pragma unroll
+  for (int k = 0; k < NP; k++) tot[k] = 0.0;
+  for (int j0 = 0; j0 < nb; j0 += 256) {
+    double v[8][NP];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int i = j0 + lane + 32 * j;
+#pragma unroll
+      for (int k = 0; k < NP; k++) v[j][k] = (i < nb) ? __ldcg(part + NP * i + k) : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+#pragma unroll
+      for (int k = 0; k < NP; k++) tot[k] += v[j][k];
+  }
+#pragma unroll
+  for (int k = 0; k < NP; k++) tot[k] = warp_sum(tot[k]);
+}
+
 // Grid total of the threads' partials v (added in their own precision within
-// a block, as the launch path's kernels do, and in FP64 across blocks, in index
-// order), handed to f, which runs in thread 0 of every block; every thread of
-// the block gets f's result.  The scalars that follow a sum (alpha, beta, the
-// stopping tests) are thus computed once per block: a double division is about
-// ten operations of the FP64 pipe, which retires two per SM per clock.
+// a block, as the launch path's kernels do, and in FP64 across blocks, in the
+// fixed order of warp_read_partials), handed to f, which runs in thread 0 of
+// every block; every thread of the block gets f's result.  The scalars that
+// follow a sum (alpha, beta, the stopping tests) are thus computed once per
+// block: a double division is about ten operations of the FP64 pipe, which
+// retires two per SM per clock.
 template <int BS, typename T, class F>
 __device__ __forceinline__ bool grid_total_then(T v, double* part, const GridBar& bar, F f, decltype(f(0.0))& out) {
   using S = decltype(f(0.0));
   __shared__ T sh[BS / 32];
-  __shared__ double shd[BS / 32];
   __shared__ S s_out;
   const T b = block_sum<BS, T>(v, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = (double)b;
   if (!grid_barrier(bar)) return false;
-  double s = 0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += BS) s += __ldcg(part + i);
-  s = block_sum<BS, double>(s, shd);
-  if (threadIdx.x == 0) s_out = f(s);
+  if (threadIdx.x < 32) {
+    double s[1];
+    warp_read_partials<1>(part, s);
+    if (threadIdx.x == 0) s_out = f(s[0]);
+  }
   __syncthreads();
   out = s_out;
   return true;
@@ -492,14 +521,9 @@ __device__ __forceinline__ double2 grid_read2(const double* part) {
   __shared__ double2 s_out;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (wid == 0) {
-    double a = 0, b = 0;
-    for (int i = lane; i < (int)gridDim.x; i += 32) {
-      a += __ldcg(part + 2 * i);
-      b += __ldcg(part + 2 * i + 1);
-    }
-    a = warp_sum(a);
-    b = warp_sum(b);
-    if (lane == 0) s_out = make_double2(a, b);
+    double t[2];
+    warp_read_partials<2>(part, t);
+    if (lane == 0) s_out = make_double2(t[0], t[1]);
   }
   __syncthreads();
   return s_out;
