@@ -48,24 +48,22 @@ __device__ __forceinline__ unsigned& barrier_epoch() {
 // passed once the count reaches k * nblocks (the grid's blocks).  Each block
 // adds its arrival without waiting for the atomic's result and polls the
 // count, so no block has to finish the barrier for the others.  After `limit`
-// polls a block gives up and returns false.
-__device__ __forceinline__ bool grid_barrier_n(const GridBar& b, unsigned nblocks, long long limit) {
-  __shared__ int s_ok;
-  if (nblocks == 1) {  // a one-block grid (small lattices): the block barrier orders its global writes
-    __syncthreads();
-    return true;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
+// polls a block gives up.
+//
+// warp0_grid_wait is the barrier's core, run by warp 0 after a block barrier
+// that follows the block's writes; it returns false in every lane if the wait
+// gave up.  The arrival (lane 0) is a release and each poll an acquire at GPU
+// scope: the block's writes, ordered before lane 0 by that block barrier, are
+// visible to every block that sees the count complete.  The warp barrier hands
+// the acquire on to the other lanes, and the caller's next block barrier to the
+// other warps.  Measured 0.35 us faster per barrier than a fence, a relaxed
+// atomic and a second fence, with the same 152 blocks.  A one-block grid (small
+// lattices) needs no arrival: its block barrier orders its global writes.
+__device__ __forceinline__ bool warp0_grid_wait(const GridBar& b, unsigned nblocks, long long limit) {
+  int ok = 1;
+  if (nblocks > 1 && (threadIdx.x & 31) == 0) {
     const unsigned target = (barrier_epoch() += 1) * nblocks;
-    // The arrival is a release and each poll an acquire at GPU scope: the
-    // block's writes, ordered before thread 0 by the block barrier above, are
-    // visible to every block that sees the count complete, and the block
-    // barrier below hands the acquire on to the block's other threads.
-    // Measured 0.35 us faster per barrier than a fence, a relaxed atomic and a
-    // second fence, with the same 152 blocks.
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(b.count) : "memory");
-    int ok = 1;
     long long spins = 0;
     while (true) {
       unsigned c;
@@ -77,7 +75,17 @@ __device__ __forceinline__ bool grid_barrier_n(const GridBar& b, unsigned nblock
       }
       __nanosleep(32);
     }
-    s_ok = ok;
+  }
+  __syncwarp();
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+__device__ __forceinline__ bool grid_barrier_n(const GridBar& b, unsigned nblocks, long long limit) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const bool ok = warp0_grid_wait(b, nblocks, limit);
+    if (threadIdx.x == 0) s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;
@@ -131,22 +139,33 @@ __device__ __forceinline__ void warp_read_partials(const double* part, double (&
 // follow a sum (alpha, beta, the stopping tests) are thus computed once per
 // block: a double division is about ten operations of the FP64 pipe, which
 // retires two per SM per clock.
+// Two block barriers in all: one after the warps' sums (it also orders the
+// block's writes before the arrival), one to hand the result to the block.
 template <int BS, typename T, class F>
 __device__ __forceinline__ bool grid_total_then(T v, double* part, const GridBar& bar, F f, decltype(f(0.0))& out) {
   using S = decltype(f(0.0));
   __shared__ T sh[BS / 32];
   __shared__ S s_out;
-  const T b = block_sum<BS, T>(v, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = (double)b;
-  if (!grid_barrier(bar)) return false;
-  if (threadIdx.x < 32) {
-    double s[1];
-    warp_read_partials<1>(part, s);
-    if (threadIdx.x == 0) s_out = f(s[0]);
+  __shared__ int s_ok;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    T b = (lane < BS / 32) ? sh[lane] : T(0);
+    b = warp_sum(b);
+    if (lane == 0) part[blockIdx.x] = (double)b;
+    const bool ok = warp0_grid_wait(bar, gridDim.x, kBarrierSpinLimit);
+    if (ok) {
+      double s[1];
+      warp_read_partials<1>(part, s);
+      if (lane == 0) s_out = f(s[0]);
+    }
+    if (lane == 0) s_ok = ok;
   }
   __syncthreads();
   out = s_out;
-  return true;
+  return s_ok != 0;
 }
 
 template <int BS>
@@ -488,12 +507,15 @@ __device__ __forceinline__ void cgcg_update(const Geo& g, float4* __restrict__ r
   }
 }
 
-// Block sums of a pair of partials (gamma, delta) in FP32, written to part as
-// FP64 (grid_publish2); after the grid barrier that follows, every block adds
-// all blocks' pairs in index order (grid_read2).
+// Grid totals of a pair of partials (gamma, delta): block sums in FP32,
+// written to part as FP64 pairs; after the grid barrier, warp 0 of every block
+// adds all blocks' pairs (warp_read_partials) and hands the totals to the block
+// through one block barrier, two block barriers in all.
 template <int BS>
-__device__ __forceinline__ void grid_publish2(float va, float vb, double* part) {
+__device__ __forceinline__ bool grid_total2(float va, float vb, double* part, const GridBar& bar, double2& out) {
   __shared__ float sha[BS / 32], shb[BS / 32];
+  __shared__ double2 s_out;
+  __shared__ int s_ok;
   va = warp_sum(va);
   vb = warp_sum(vb);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -510,25 +532,18 @@ __device__ __forceinline__ void grid_publish2(float va, float vb, double* part) 
       part[2 * blockIdx.x] = (double)a;
       part[2 * blockIdx.x + 1] = (double)b;
     }
-  }
-}
-// Warp 0 adds the pairs (each lane the blocks lane, lane + 32, ..., then a
-// fixed shuffle tree) and hands the totals to the block through one block
-// barrier: measured 1.7% faster per iteration at 2048^2 than a reduction over
-// all warps with three block barriers.
-template <int BS>
-__device__ __forceinline__ double2 grid_read2(const double* part) {
-  __shared__ double2 s_out;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (wid == 0) {
-    double t[2];
-    warp_read_partials<2>(part, t);
-    if (lane == 0) s_out = make_double2(t[0], t[1]);
+    const bool ok = warp0_grid_wait(bar, gridDim.x, kBarrierSpinLimit);
+    if (ok) {
+      double t[2];
+      warp_read_partials<2>(part, t);
+      if (lane == 0) s_out = make_double2(t[0], t[1]);
+    }
+    if (lane == 0) s_ok = ok;
   }
   __syncthreads();
-  return s_out;
+  out = s_out;
+  return s_ok != 0;
 }
-
 // The FP64 reliable update shared by the single-reduction kernels:
 // x += xs, xs = 0; r = (float)(b - M^dag M x) with |b - M^dag M x|^2 summed
 // into rt.  False if a grid barrier gave up.
@@ -617,11 +632,7 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgcg(PcgMxArgs a) {
       de = fmaf(u.x, u.x, fmaf(u.y, u.y, de));
     };
     stencil_mdagm<MU0>(g, a.km32, a.kd32, ld, a.Wt32, a.Wx32, epi);
-    double* pp = part();
-    grid_publish2<BS>(ga, de, pp);
-    if (!grid_barrier(a.bar)) return false;
-    gd = grid_read2<BS>(pp);
-    return true;
+    return grid_total2<BS>(ga, de, part(), a.bar, gd);
   };
   double gam = 0, alpha = 0, beta = 0;
   if (status < 0) {
