@@ -81,6 +81,34 @@ def test_persistent_1024(tg, oracle_lib, precision):
         assert res.reliable_updates >= 1
 
 
+@pytest.mark.parametrize("form", ["fp64", "twosum", "onesum"])
+def test_grid_of_more_than_256_blocks(tg, oracle_lib, monkeypatch, form):
+    """256-thread blocks, two per SM, on a lattice whose work fills them all:
+    the grid has more blocks than warp 0 reads in one round of partial loads
+    (256), so every grid sum takes two.  The solution against the oracle and
+    against the default 512-thread shape."""
+    nt, nx = 1024, 512
+    rng = np.random.default_rng(77)
+    A = rng.normal(0, 0.3, (nt, nx, 2))
+    b = cplx(rng, (nt, nx))
+    L = tg.Lattice(nt, nx, 0.05, 0.6, 0.0, -1, 1)
+    L.set_gauge(A)
+    prec = 0 if form == "fp64" else 1
+    monkeypatch.setenv("TG_MIXED_CG", "twosum" if form == "fp64" else form)
+    cp = tg.cg_params(rel_tol=1e-10, abs_tol2=0, precision=prec, ru_interval=50, solver=PERSISTENT)
+    out = {}
+    for block in ("256", "512"):
+        monkeypatch.setenv("TG_PCG_BLOCK", block)
+        out[block] = L.fmdm_invert_cg(b, cp)
+    (x2, r2), (x5, r5) = out["256"], out["512"]
+    assert r2.status == r5.status == 0
+    assert abs(r2.iterations - r5.iterations) <= max(3, r5.iterations // 50)
+    o = oracle_lib.Oracle(nt, nx, 0.05, 0.6, 0.0, -1, 1)
+    true = np.linalg.norm(b - o.Mdag(A, o.M(A, x2))) / np.linalg.norm(b)
+    assert true < 1.5e-10, true
+    assert rel(x2, x5) < 1e-6   # both at 1e-10 residual; M^dag M at m 0.05 has a condition number of ~2000
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_persistent_edge_cases(tg, precision):
     rng = np.random.default_rng(9)
