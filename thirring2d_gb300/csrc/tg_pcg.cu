@@ -82,6 +82,10 @@ __device__ __forceinline__ bool warp0_grid_wait(const GridBar& b, unsigned nbloc
 
 __device__ __forceinline__ bool grid_barrier_n(const GridBar& b, unsigned nblocks, long long limit) {
   __shared__ int s_ok;
+  if (nblocks == 1) {
+    __syncthreads();
+    return true;
+  }
   __syncthreads();
   if (threadIdx.x < 32) {
     const bool ok = warp0_grid_wait(b, nblocks, limit);
@@ -102,6 +106,15 @@ __global__ void k_barrier_check(GridBar b, unsigned phantom, long long limit, in
   if (threadIdx.x == 0) barrier_epoch() = 0;
   const bool ok = grid_barrier_n(b, gridDim.x + phantom, limit);
   if (blockIdx.x == 0 && threadIdx.x == 0) *status = ok ? TG_OK : TG_E_TIMEOUT;
+}
+
+// Loads of vectors that the solve itself writes.  Across blocks they go to L2
+// (ld.global.cg), so no SM reads a stale L1 line; in a one-block grid (ONE)
+// the block barriers order every write before every later read, and the loads
+// may hit L1: a 16^2 lattice's vectors (a few tens of KB) then stay on chip.
+template <bool ONE, typename T> __device__ __forceinline__ T ldv(const T* p) {
+  if constexpr (ONE) return *p;
+  else return __ldcg(p);
 }
 
 // Warp 0's read of the blocks' partials after a grid barrier: NP values per
@@ -154,14 +167,21 @@ __device__ __forceinline__ bool grid_total_then(T v, double* part, const GridBar
   if (wid == 0) {
     T b = (lane < BS / 32) ? sh[lane] : T(0);
     b = warp_sum(b);
-    if (lane == 0) part[blockIdx.x] = (double)b;
-    const bool ok = warp0_grid_wait(bar, gridDim.x, kBarrierSpinLimit);
-    if (ok) {
-      double s[1];
-      warp_read_partials<1>(part, s);
-      if (lane == 0) s_out = f(s[0]);
+    if (gridDim.x == 1) {  // a one-block grid: its total is the grid's, no round trip through memory
+      if (lane == 0) {
+        s_out = f((double)b);
+        s_ok = 1;
+      }
+    } else {
+      if (lane == 0) part[blockIdx.x] = (double)b;
+      const bool ok = warp0_grid_wait(bar, gridDim.x, kBarrierSpinLimit);
+      if (ok) {
+        double s[1];
+        warp_read_partials<1>(part, s);
+        if (lane == 0) s_out = f(s[0]);
+      }
+      if (lane == 0) s_ok = ok;
     }
-    if (lane == 0) s_ok = ok;
   }
   __syncthreads();
   out = s_out;
@@ -220,7 +240,7 @@ __device__ __forceinline__ double stop_of(double rr0, double rel_tol, double abs
 // ---------------------------------------------------------------------------
 // FP64: the iteration of k_cg1 + k_cg2_64 (unit-mass form when UNIT)
 // ---------------------------------------------------------------------------
-template <int BS, bool MU0, bool UNIT>
+template <int BS, bool MU0, bool UNIT, bool ONE = false>
 __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcg64(Pcg64Args a) {
   if (threadIdx.x == 0) barrier_epoch() = 0;
   const Geo& g = a.g;
@@ -251,7 +271,7 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcg64(Pcg64Args a) {
     double2* p_new = half ? a.p0 : a.p1;
     double va = 0;
     auto ld_a = [&](int i) {
-      const double2 rv = __ldcg(a.r + i), pv = __ldcg(p_old + i);
+      const double2 rv = ldv<ONE>(a.r + i), pv = ldv<ONE>(p_old + i);
       return make_double2(fma(beta, pv.x, rv.x), fma(beta, pv.y, rv.y));
     };
     auto epi_a = [&](int s, double2 o, double2 pc) {
@@ -271,9 +291,9 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcg64(Pcg64Args a) {
     }
     const double alpha = st.alpha, ax = st.ax;
     double vb = 0;
-    auto ld_b = [&](int i) { return __ldcg(a.Mp + i); };
+    auto ld_b = [&](int i) { return ldv<ONE>(a.Mp + i); };
     auto epi_b = [&](int s, double2 ap, double2) {
-      double2 xv = __ldcg(a.x + s), pv = __ldcg(p_new + s), rv = __ldcg(a.r + s);
+      double2 xv = ldv<ONE>(a.x + s), pv = ldv<ONE>(p_new + s), rv = ldv<ONE>(a.r + s);
       xv.x += ax * pv.x;
       xv.y += ax * pv.y;
       rv.x -= alpha * ap.x;
@@ -309,7 +329,7 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcg64(Pcg64Args a) {
 // Mixed: the iteration of k_cg1<float> + k_cgmx2, and the reliable update of
 // k_ru1..3 with the same triggers and restart rule.
 // ---------------------------------------------------------------------------
-template <int BS, bool MU0>
+template <int BS, bool MU0, bool ONE = false>
 __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
   if (threadIdx.x == 0) barrier_epoch() = 0;
   const Geo& g = a.g;
@@ -345,7 +365,7 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
     float2* p_new = half ? a.p0 : a.p1;
     float va = 0;
     auto ld_a = [&](int i) {
-      const float2 rv = __ldcg(a.r + i), pv = __ldcg(p_old + i);
+      const float2 rv = ldv<ONE>(a.r + i), pv = ldv<ONE>(p_old + i);
       return make_float2(fmaf(bf, pv.x, rv.x), fmaf(bf, pv.y, rv.y));
     };
     auto epi_a = [&](int s, float2 o, float2 pc) {
@@ -361,9 +381,9 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
       break;
     }
     float vb = 0;
-    auto ld_b = [&](int i) { return __ldcg(a.Mp + i); };
+    auto ld_b = [&](int i) { return ldv<ONE>(a.Mp + i); };
     auto epi_b = [&](int s, float2 ap, float2) {
-      float2 xv = __ldcg(a.xs + s), pv = __ldcg(p_new + s), rv = __ldcg(a.r + s);
+      float2 xv = ldv<ONE>(a.xs + s), pv = ldv<ONE>(p_new + s), rv = ldv<ONE>(a.r + s);
       xv.x = fmaf(af, pv.x, xv.x);
       xv.y = fmaf(af, pv.y, xv.y);
       rv.x = fmaf(-af, ap.x, rv.x);
@@ -392,8 +412,8 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
     if (!e.need) continue;
     // reliable update: x += xs, xs = 0; r = b - M^dag M x in FP64; rs = (float) r
     TG_SITES(s, g.V) {
-      const float2 d = __ldcg(a.xs + s);
-      double2 xv = __ldcg(a.x + s);
+      const float2 d = ldv<ONE>(a.xs + s);
+      double2 xv = ldv<ONE>(a.x + s);
       xv.x += (double)d.x;
       xv.y += (double)d.y;
       a.x[s] = xv;
@@ -403,7 +423,7 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
       status = TG_E_TIMEOUT;
       break;
     }
-    auto ld_x = [&](int i) { return __ldcg(a.x + i); };
+    auto ld_x = [&](int i) { return ldv<ONE>(a.x + i); };
     auto epi_x = [&](int s, double2 o, double2) { a.tmp[s] = o; };
     stencil_ld<double, 0, MU0>(g, a.km, ld_x, a.Wt, a.Wx, epi_x);
     if (!grid_barrier(a.bar)) {
@@ -411,7 +431,7 @@ __global__ void __launch_bounds__(BS, pcg_min_blocks(BS)) k_pcgmx(PcgMxArgs a) {
       break;
     }
     double vt = 0;
-    auto ld_t = [&](int i) { return __ldcg(a.tmp + i); };
+    auto ld_t = [&](int i) { return ldv<ONE>(a.tmp + i); };
     auto epi_t = [&](int s, double2 ap, double2) {
       const double2 bb = a.b[s];
       const double2 rv = make_double2(bb.x - ap.x, bb.y - ap.y);
@@ -749,24 +769,33 @@ int pcg_block_override() {
   return (v == 512 || v == 256) ? v : 0;
 }
 
-// the 512-thread kernel when its blocks fill every SM, else the 256-thread one
-template <class K512, class K256, class Args>
-cudaError_t pcg_launch(const Geo& g, K512 k512, K256 k256, cudaStream_t s, const Args& a) {
+// the 512-thread kernel when its blocks fill every SM, else the 256-thread one;
+// a lattice whose work fits one 256-thread block runs the one-block instance
+// (k1; L1-cached loads, block totals kept on chip)
+template <class K512, class K256, class K1, class Args>
+cudaError_t pcg_launch(const Geo& g, K512 k512, K256 k256, K1 k1, cudaStream_t s, const Args& a) {
   const int r512 = pcg_resident(k512, 512);
   const int force = pcg_block_override();
   if (force == 512) return coop_launch(k512, std::min(r512, kPcgMaxGrid), 512, s, a);
   if (force == 0 && pcg_work(g, 512) >= r512) return coop_launch(k512, pcg_grid(g, r512, 512), 512, s, a);
-  return coop_launch(k256, pcg_grid(g, pcg_resident(k256, 256), 256), 256, s, a);
+  const int grid = pcg_grid(g, pcg_resident(k256, 256), 256);
+  if (grid == 1) return coop_launch(k1, 1, 256, s, a);
+  return coop_launch(k256, grid, 256, s, a);
 }
 
 cudaError_t pcg64(cudaStream_t s, bool mu0, Pcg64Args a) {
   const bool unit = a.inv_m2 != 0.0;
   if (mu0) {
-    if (unit) return pcg_launch(a.g, k_pcg64<512, true, true>, k_pcg64<256, true, true>, s, a);
-    return pcg_launch(a.g, k_pcg64<512, true, false>, k_pcg64<256, true, false>, s, a);
+    if (unit)
+      return pcg_launch(a.g, k_pcg64<512, true, true>, k_pcg64<256, true, true>, k_pcg64<256, true, true, true>, s, a);
+    return pcg_launch(a.g, k_pcg64<512, true, false>, k_pcg64<256, true, false>, k_pcg64<256, true, false, true>, s,
+                      a);
   }
-  if (unit) return pcg_launch(a.g, k_pcg64<512, false, true>, k_pcg64<256, false, true>, s, a);
-  return pcg_launch(a.g, k_pcg64<512, false, false>, k_pcg64<256, false, false>, s, a);
+  if (unit)
+    return pcg_launch(a.g, k_pcg64<512, false, true>, k_pcg64<256, false, true>, k_pcg64<256, false, true, true>, s,
+                      a);
+  return pcg_launch(a.g, k_pcg64<512, false, false>, k_pcg64<256, false, false>, k_pcg64<256, false, false, true>, s,
+                    a);
 }
 
 cudaError_t barrier_check(cudaStream_t s, unsigned* count, unsigned phantom, long long limit, int* status) {
@@ -783,14 +812,14 @@ cudaError_t barrier_check(cudaStream_t s, unsigned* count, unsigned phantom, lon
 }
 
 cudaError_t pcgmx(cudaStream_t s, bool mu0, PcgMxArgs a) {
-  if (mu0) return pcg_launch(a.g, k_pcgmx<512, true>, k_pcgmx<256, true>, s, a);
-  return pcg_launch(a.g, k_pcgmx<512, false>, k_pcgmx<256, false>, s, a);
+  if (mu0) return pcg_launch(a.g, k_pcgmx<512, true>, k_pcgmx<256, true>, k_pcgmx<256, true, true>, s, a);
+  return pcg_launch(a.g, k_pcgmx<512, false>, k_pcgmx<256, false>, k_pcgmx<256, false, true>, s, a);
 }
 
 cudaError_t pcgcg(cudaStream_t s, bool mu0, PcgMxArgs a) {
   if (!a.g.march) return cudaErrorInvalidValue;
-  if (mu0) return pcg_launch(a.g, k_pcgcg<512, true>, k_pcgcg<256, true>, s, a);
-  return pcg_launch(a.g, k_pcgcg<512, false>, k_pcgcg<256, false>, s, a);
+  if (mu0) return pcg_launch(a.g, k_pcgcg<512, true>, k_pcgcg<256, true>, k_pcgcg<256, true>, s, a);
+  return pcg_launch(a.g, k_pcgcg<512, false>, k_pcgcg<256, false>, k_pcgcg<256, false>, s, a);
 }
 
 }  // namespace tg
