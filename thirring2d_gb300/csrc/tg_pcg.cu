@@ -9,7 +9,8 @@
 // uniform across the grid without a broadcast.  Two partial arrays alternate,
 // so a block that races ahead never overwrites partials another block is
 // still reading.  Vectors that other blocks write during the solve are read
-// with ld.global.cg (L2), so no SM sees a stale L1 line.  Each block marches
+// with ld.global.cg (L2), so no SM sees a stale L1 line (a one-block grid reads
+// them through L1, see ldv).  Each block marches
 // the same row ranges in every phase (tg_stencil.cuh).
 //
 // The barrier's wait is bounded: after kBarrierSpinLimit polls a block gives
@@ -119,10 +120,9 @@ template <bool ONE, typename T> __device__ __forceinline__ T ldv(const T* p) {
 
 // Warp 0's read of the blocks' partials after a grid barrier: NP values per
 // block, part[NP * i + k].  Each lane adds the blocks lane, lane + 32, ... in
-// index order, with the loads of up to 256 blocks in flight at once (a loop
-// would wait one L2 round trip per block), then a fixed shuffle tree; the
-// totals are valid in lane 0.  Measured 0.17 us faster per sum than a read by
-// all threads with a block-wide tree.
+// index order, with the loads of up to 256 blocks issued before any is used,
+// then a fixed shuffle tree; the totals are valid in lane 0.  Measured 0.17 us
+// faster per sum than a read by all threads with a block-wide tree.
 template <int NP>
 __device__ __forceinline__ void warp_read_partials(const double* part, double (&tot)[NP]) {
   const int lane = threadIdx.x & 31, nb = (int)gridDim.x;
