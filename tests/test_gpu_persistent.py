@@ -109,6 +109,34 @@ def test_grid_of_more_than_256_blocks(tg, oracle_lib, monkeypatch, form):
     assert rel(x2, x5) < 1e-6   # both at 1e-10 residual; M^dag M at m 0.05 has a condition number of ~2000
 
 
+@pytest.mark.parametrize("case", ["heavy", "tiny", "large"])
+def test_mixed_fixed_point_sums_leave_their_scale(tg, oracle_lib, case):
+    """The mixed solver adds its iteration sums as integers at a power-of-two
+    scale that follows the last total of the same kind.  Systems whose sums
+    leave that scale: a heavy mass (the first |Mp|^2 is ~2500 |b|^2, past a
+    block's 256-fold headroom, so every block takes the exact path), and
+    right-hand sides of norm 1e-15 and 1e+15 per site.  Each solve against the
+    FP64 solve and the oracle's residual."""
+    nt, nx = 128, 128   # a multi-block grid (fixed-point sums)
+    m = 50.0 if case == "heavy" else 0.2
+    amp = {"heavy": 1.0, "tiny": 1e-15, "large": 1e15}[case]
+    rng = np.random.default_rng(31)
+    A = rng.normal(0, 0.4, (nt, nx, 2))
+    b = amp * cplx(rng, (nt, nx))
+    L = tg.Lattice(nt, nx, m, 0.5, 0.0, -1, 1)
+    L.set_gauge(A)
+    out = {}
+    for prec in (0, 1):
+        out[prec] = L.fmdm_invert_cg(b, tg.cg_params(rel_tol=1e-10, abs_tol2=0, precision=prec, ru_interval=50,
+                                                    solver=PERSISTENT))
+    (x64, r64), (xmx, rmx) = out[0], out[1]
+    assert r64.status == rmx.status == 0
+    assert abs(rmx.iterations - r64.iterations) <= max(3, r64.iterations // 10)
+    assert rel(xmx, x64) < 1e-7
+    o = oracle_lib.Oracle(nt, nx, m, 0.5, 0.0, -1, 1)
+    assert np.linalg.norm(b - o.Mdag(A, o.M(A, xmx))) / np.linalg.norm(b) < 1.5e-10
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_persistent_edge_cases(tg, precision):
     rng = np.random.default_rng(9)

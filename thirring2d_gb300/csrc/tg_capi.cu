@@ -123,7 +123,7 @@ struct tg_lattice {
   CgLog* log = nullptr;
   TrajStats* ts = nullptr;
   Red red{};
-  unsigned* bar = nullptr;      // persistent solver: grid barrier {count, gen}
+  unsigned* bar = nullptr;      // persistent solver: barrier words [kBarWords]
   double* pcg_part = nullptr;   // and its partial sums [4 * kPcgMaxGrid]
 
   double* h_stage = nullptr;  // pinned, 2*V*kMaxPf doubles... sized at create
@@ -306,8 +306,8 @@ bool use_single_reduction(const tg_lattice* L) {
 // arrival count is cleared first, so a solve that timed out leaves no trace.
 int enqueue_pcg(tg_lattice* L, cudaStream_t s, const tg_cg_params& cp, const double2* b, double2* x, int log_index) {
   const Links lk = links(L);
-  const GridBar bar{L->bar};
-  TG_CK(cudaMemsetAsync(L->bar, 0, sizeof(unsigned), s));
+  const GridBar bar{L->bar, reinterpret_cast<unsigned long long*>(L->bar + 2)};
+  TG_CK(cudaMemsetAsync(L->bar, 0, kBarWords * sizeof(unsigned), s));
   cudaError_t e;
   if (cp.precision == TG_PREC_MIXED) {
     PcgMxArgs a{};
@@ -796,7 +796,7 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
     if ((rc = dmalloc(pp, n)) != TG_OK) return bail(rc);
   if ((rc = dmalloc(&L->st, 1)) != TG_OK || (rc = dmalloc(&L->log, kMaxLog)) != TG_OK ||
       (rc = dmalloc(&L->ts, 1)) != TG_OK || (rc = dmalloc(&L->red.partials, (size_t)nblocks((int)V) + 32)) != TG_OK ||
-      (rc = dmalloc(&L->red.counter, 1)) != TG_OK || (rc = dmalloc(&L->bar, 2)) != TG_OK ||
+      (rc = dmalloc(&L->red.counter, 1)) != TG_OK || (rc = dmalloc(&L->bar, kBarWords)) != TG_OK ||
       (rc = dmalloc(&L->pcg_part, 4 * (size_t)kPcgMaxGrid)) != TG_OK)
     return bail(rc);
   if ((rc = ensure_pf(L, 1)) != TG_OK) return bail(rc);
@@ -809,7 +809,7 @@ int tg_create(const tg_lattice_params* p, tg_lattice** out) {
   if (cudaMemsetAsync(L->A, 0, n * sizeof(double2), L->stream) != cudaSuccess ||
       cudaMemsetAsync(L->noise, 0, n * sizeof(double2), L->stream) != cudaSuccess ||
       cudaMemsetAsync(L->red.counter, 0, sizeof(unsigned), L->stream) != cudaSuccess ||
-      cudaMemsetAsync(L->bar, 0, 2 * sizeof(unsigned), L->stream) != cudaSuccess ||
+      cudaMemsetAsync(L->bar, 0, kBarWords * sizeof(unsigned), L->stream) != cudaSuccess ||
       cudaMemsetAsync(L->ts, 0, sizeof(TrajStats), L->stream) != cudaSuccess ||
       cudaMemsetAsync(L->st, 0, sizeof(CgState), L->stream) != cudaSuccess)
     return bail(fail(TG_E_CUDA, "initial memset failed"));

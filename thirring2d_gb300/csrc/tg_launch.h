@@ -116,8 +116,13 @@ void lu_logdet(cudaStream_t s, int V, int nmat, double2* mats, double* out);
 // ---------------------------------------------------------------------------
 // Persistent CG (tg_pcg.cu): one cooperative launch per solve
 // ---------------------------------------------------------------------------
-struct GridBar {       // grid barrier: monotonic arrival count (must be 0 at launch)
-  unsigned* count;
+// The persistent solver's barrier words, all 0 at launch: the arrival count,
+// a spare word, then the two 64-bit words of the fixed-point sums (one per
+// kind of iteration sum of the mixed CG; see tg_pcg.cu).
+constexpr int kBarWords = 6;
+struct GridBar {
+  unsigned* count;           // grid barrier: monotonic arrival count
+  unsigned long long* fx;    // fixed-point sums: 2 words (count + 2)
 };
 // largest persistent grid; partial sums: 4 * kPcgMaxGrid doubles (two alternating
 // arrays of (gamma, delta) pairs in the single-reduction CG)
