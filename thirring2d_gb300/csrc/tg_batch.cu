@@ -11,7 +11,7 @@ template <int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_batch_trajectory(const BatchChain* __restrict__ chains,
                                                                const int* __restrict__ order, int n,
                                                                BatchFields F, BatchTraj P, ChainResult* results,
-                                                               unsigned* queue) {
+                                                               unsigned long long* queue) {
   batch_trajectory_body<BS, MINB, BlockTeam>(chains, order, n, F, P, results, queue);
 }
 
@@ -48,7 +48,7 @@ static const void* batch_kernel_of(int cfg) {
 }
 
 static void launch_blocks(cudaStream_t s, int cfg, int grid, const BatchChain* chains, const int* order, int n,
-                          const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue) {
+                          const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned long long* queue) {
   switch (cfg) {
     case 0: k_batch_trajectory<128, 8><<<grid, 128, 0, s>>>(chains, order, n, F, P, results, queue); break;
     case 1: k_batch_trajectory<256, 4><<<grid, 256, 0, s>>>(chains, order, n, F, P, results, queue); break;
@@ -68,8 +68,27 @@ int batch_teams(int cfg, int sms) {
   return nb * sms;
 }
 
+int batch_filler_blocks(int cfg, int sms) {
+  const BatchCfg& c = kBatchCfgs[cfg];
+  if (c.cluster <= 1 || c.solo_sites <= 0) return 0;
+  const int clusters = batch_cluster_max(cluster_kernel_of(cfg));
+  return std::max(0, sms - clusters * c.cluster);
+}
+
+void batch_filler_launch(cudaStream_t s, int cfg, int blocks, const BatchChain* chains, const int* order, int n,
+                         const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned long long* queue) {
+  BatchTraj f = P;
+  f.from_back = 1;
+  // the one-block instance of the cluster kernel's block size: its solo chains
+  // run the same code, so a chain's result does not depend on which block ran it
+  if (kBatchCfgs[cfg].block == 512)
+    k_batch_trajectory<512, 1><<<blocks, 512, 0, s>>>(chains, order, n, F, f, results, queue);
+  else
+    k_batch_trajectory<256, 1><<<blocks, 256, 0, s>>>(chains, order, n, F, f, results, queue);
+}
+
 void batch_trajectory(cudaStream_t s, int cfg, int sms, const BatchChain* chains, const int* order, int n,
-                      const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue) {
+                      const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned long long* queue) {
   const int teams = std::min(n, std::max(1, batch_teams(cfg, sms)));
   if (kBatchCfgs[cfg].cluster > 1)
     batch_cluster_launch(s, cluster_kernel_of(cfg), teams, chains, order, n, F, P, results, queue);

@@ -35,6 +35,9 @@ struct BatchTraj {
   // cluster instances: from this queue position on, every block of a cluster
   // runs chains of its own (n: never)
   int solo_from;
+  // 1 for the filler blocks beside a cluster launch: they take chains from the
+  // back of the queue, at or after solo_from only
+  int from_back;
 };
 
 // Per-chain outcome of a trajectory; `traj` is the chain's Philox trajectory
@@ -55,9 +58,20 @@ struct BatchCfg {
 constexpr int kBatchNumCfgs = 15;
 extern const BatchCfg kBatchCfgs[kBatchNumCfgs];
 
+// The work queue is one 64-bit word (0 at launch): the low half counts the
+// chains taken from its front (teams, largest estimated cost first), the high
+// half those taken from its back (filler blocks, the cheapest chains).
+//
 // Launches instance cfg over n chains with as many teams as can be resident.
 void batch_trajectory(cudaStream_t s, int cfg, int sms, const BatchChain* chains, const int* order, int n,
-                      const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue);
+                      const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned long long* queue);
+// Cluster instances with solo chains leave SMs that hold no whole cluster idle
+// (152 SMs take 36 clusters of 4): one-block teams of the same block size run
+// there, concurrently on stream s, taking solo chains from the back of the
+// queue.  batch_filler_blocks gives their number (0: none for this instance).
+int batch_filler_blocks(int cfg, int sms);
+void batch_filler_launch(cudaStream_t s, int cfg, int blocks, const BatchChain* chains, const int* order, int n,
+                         const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned long long* queue);
 // teams (blocks or clusters) of instance cfg that can be resident at once (0: cannot launch)
 int batch_teams(int cfg, int sms);
 // the tuned instance as reported to callers: block * 100 + 10 * cluster (if > 1)
@@ -69,6 +83,7 @@ inline int batch_cfg_id(const BatchCfg& c) {
 // tg_batch_cluster.cu: instance `which` (0: 512 x 2 blocks, 1: 512 x 4, 2: 256 x 4)
 int batch_cluster_max(int which);
 void batch_cluster_launch(cudaStream_t s, int which, int clusters, const BatchChain* chains, const int* order, int n,
-                          const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue);
+                          const BatchFields& F, const BatchTraj& P, ChainResult* results,
+                          unsigned long long* queue);
 
 }  // namespace tg

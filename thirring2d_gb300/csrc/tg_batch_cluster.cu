@@ -10,7 +10,7 @@ namespace tg {
 template <int BS, int CL>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BS, 1)
     k_batch_cluster(const BatchChain* __restrict__ chains, const int* __restrict__ order, int n, BatchFields F,
-                    BatchTraj P, ChainResult* results, unsigned* queue) {
+                    BatchTraj P, ChainResult* results, unsigned long long* queue) {
   batch_trajectory_body<BS, 1, ClusterTeam<CL>>(chains, order, n, F, P, results, queue);
 }
 
@@ -36,7 +36,7 @@ int batch_cluster_max(int which) {
 }
 
 void batch_cluster_launch(cudaStream_t s, int which, int clusters, const BatchChain* chains, const int* order, int n,
-                          const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned* queue) {
+                          const BatchFields& F, const BatchTraj& P, ChainResult* results, unsigned long long* queue) {
   switch (which) {
     case 0: k_batch_cluster<512, 2><<<clusters * 2, 512, 0, s>>>(chains, order, n, F, P, results, queue); break;
     case 1: k_batch_cluster<512, 4><<<clusters * 4, 512, 0, s>>>(chains, order, n, F, P, results, queue); break;

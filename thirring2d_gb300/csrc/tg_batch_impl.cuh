@@ -512,10 +512,36 @@ __device__ __forceinline__ void fill_ctx(ChainCtx& c, const BatchChain& b, const
     c.ps2 = F.ps2 + o; c.Mps = F.Mps + o;
 }
 
+// The two ends of the work queue (one 64-bit word: front draws in the low
+// half, back draws in the high half).  A draw succeeds while front + back < n
+// before it: in the word's order of updates every position is then handed out
+// once, to whichever end reaches it first.  Both return n when nothing is left.
+__device__ __forceinline__ int queue_front(unsigned long long* queue, int n) {
+  const unsigned long long old = atomicAdd(queue, 1ull);
+  const long long f = (long long)(old & 0xffffffffull), b = (long long)(old >> 32);
+  return (f + b < n) ? (int)f : n;
+}
+// From the back, but only positions at or after `lo`: the test and the draw are
+// one compare-and-swap, so a refused position stays with the front.  The
+// retries are bounded; a block that gives up leaves the rest to the front.
+__device__ __forceinline__ int queue_back(unsigned long long* queue, int n, int lo) {
+  unsigned long long old = *reinterpret_cast<volatile unsigned long long*>(queue);
+  for (int tries = 0; tries < (1 << 20); tries++) {
+    const long long f = (long long)(old & 0xffffffffull), b = (long long)(old >> 32);
+    const long long t = (long long)n - 1 - b;
+    if (f + b >= n || t < lo) return n;
+    const unsigned long long seen = atomicCAS(queue, old, old + (1ull << 32));
+    if (seen == old) return (int)t;
+    old = seen;
+  }
+  return n;
+}
+
 template <int BS, int MINB, class T>
 __device__ __forceinline__ void batch_trajectory_body(const BatchChain* __restrict__ chains,
                                                       const int* __restrict__ order, int n, const BatchFields& F,
-                                                      const BatchTraj& P, ChainResult* results, unsigned* queue) {
+                                                      const BatchTraj& P, ChainResult* results,
+                                                      unsigned long long* queue) {
   // The chain context (geometry, couplings, ~20 field pointers) lives in shared
   // memory: kept in registers it would cost ~40 of them per thread.  Every
   // block of a team fills its own copy.
@@ -524,7 +550,8 @@ __device__ __forceinline__ void batch_trajectory_body(const BatchChain* __restri
   T::init();  // published by the first broadcast's barriers
   int q;
   while (true) {
-    if (T::rank() == 0 && threadIdx.x == 0) next = (int)atomicAdd(queue, 1u);
+    if (T::rank() == 0 && threadIdx.x == 0)
+      next = (!T::kCluster && P.from_back) ? queue_back(queue, n, P.solo_from) : queue_front(queue, n);
     q = T::broadcast(&next);
     if (q >= n || (T::kCluster && q >= P.solo_from)) break;
     const int ci = order[q];
@@ -541,7 +568,7 @@ __device__ __forceinline__ void batch_trajectory_body(const BatchChain* __restri
     int mine = (q < n && T::rank() == 0) ? q : -1;
     while (true) {
       if (mine < 0) {
-        if (threadIdx.x == 0) next = (int)atomicAdd(queue, 1u);
+        if (threadIdx.x == 0) next = queue_front(queue, n);
         __syncthreads();
         mine = next;
         if (mine >= n) break;

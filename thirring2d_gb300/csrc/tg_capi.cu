@@ -1490,11 +1490,13 @@ struct tg_batch {
   std::vector<long long> off;
   std::vector<int> order;  // the work queue: chains by estimated cost, largest first
   cudaStream_t stream = nullptr;
+  cudaStream_t filler = nullptr;               // the filler blocks' stream (batch_filler_launch)
+  cudaEvent_t fork = nullptr, join = nullptr;  // ordering it into `stream` (also under graph capture)
   BatchChain* d_chains = nullptr;
   int* d_order = nullptr;
   ChainResult* d_res = nullptr;
   ChainResult* h_res = nullptr;
-  unsigned* d_queue = nullptr;
+  unsigned long long* d_queue = nullptr;
   BatchFields F{};
   int sms = 1;
   int tuned_cfg = 1;  // index into kBatchCfgs
@@ -1524,6 +1526,7 @@ int batch_launch(tg_batch* B, const tg_batch_params& p, int cfg, cudaStream_t s)
   t.tau = p.tau;
   t.stochastic_term = p.stochastic_term;
   t.cg = BatchCg{p.cg.rel_tol, p.cg.abs_tol2, p.cg.maxiter, p.cg.precision, p.cg.ru_interval};
+  t.from_back = 0;
   // cluster instances with solo_sites: single blocks from the first queued chain that small
   t.solo_from = B->n;
   if (kBatchCfgs[cfg].cluster > 1 && kBatchCfgs[cfg].solo_sites > 0)
@@ -1532,9 +1535,21 @@ int batch_launch(tg_batch* B, const tg_batch_params& p, int cfg, cudaStream_t s)
         t.solo_from = q;
         break;
       }
-  TG_CK(cudaMemsetAsync(B->d_queue, 0, sizeof(unsigned), s));
+  TG_CK(cudaMemsetAsync(B->d_queue, 0, sizeof(unsigned long long), s));
+  // filler blocks on the SMs the clusters leave idle, on a stream forked from s
+  // after the queue's reset and joined back into s; launched after the cluster
+  // kernel, whose clusters should take their SMs first
+  const int fill = (t.solo_from < B->n) ? batch_filler_blocks(cfg, B->sms) : 0;
+  if (fill > 0) TG_CK(cudaEventRecord(B->fork, s));
   batch_trajectory(s, cfg, B->sms, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
   TG_CK(cudaGetLastError());
+  if (fill > 0) {
+    TG_CK(cudaStreamWaitEvent(B->filler, B->fork, 0));
+    batch_filler_launch(B->filler, cfg, fill, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
+    TG_CK(cudaGetLastError());
+    TG_CK(cudaEventRecord(B->join, B->filler));
+    TG_CK(cudaStreamWaitEvent(s, B->join, 0));
+  }
   return TG_OK;
 }
 
@@ -1630,7 +1645,10 @@ int tg_batch_create(const tg_chain_params* chains, int nchains, int device, tg_b
     return ca > cb;
   });
   if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&B->e0) != cudaSuccess || cudaEventCreate(&B->e1) != cudaSuccess)
+      cudaStreamCreateWithFlags(&B->filler, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&B->e0) != cudaSuccess || cudaEventCreate(&B->e1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->join, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(TG_E_CUDA, "stream/event creation failed"));
   cudaDeviceGetAttribute(&B->sms, cudaDevAttrMultiProcessorCount, device);
   if (B->sms <= 0) B->sms = 1;
@@ -1678,6 +1696,9 @@ int tg_batch_destroy(tg_batch* B) {
   if (B->h_res) cudaFreeHost(B->h_res);
   if (B->e0) cudaEventDestroy(B->e0);
   if (B->e1) cudaEventDestroy(B->e1);
+  if (B->fork) cudaEventDestroy(B->fork);
+  if (B->join) cudaEventDestroy(B->join);
+  if (B->filler) cudaStreamDestroy(B->filler);
   if (B->stream) cudaStreamDestroy(B->stream);
   delete B;
   return TG_OK;
