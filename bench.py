@@ -669,7 +669,7 @@ def run_stable(tg, torch, dev, A0, seed, flush, ntraj=4):
     return out
 
 
-def run_c1(tg, torch, dev, ntraj=200, nchains=512, batch_steps=5):
+def run_c1(tg, torch, dev, ntraj=200, nchains=512, batch_steps=20):
     """The 16^2 plain-FP64 workload as the reference runs it (periodic x, m 0.1,
     g 0.5, A ~ N(0, 0.1^2), 10 steps, tau 1): one chain on the FP64 path on the
     reference's MT stream, with the reference's CG stop (|r|^2 < 1e-30) and with
@@ -725,7 +725,7 @@ def run_c1(tg, torch, dev, ntraj=200, nchains=512, batch_steps=5):
         ms = sum(B.trajectory(bp)[0].cg_ms for _ in range(batch_steps))
         B.close()
         batch[name] = {"value": nchains * batch_steps / (ms / 1e3), "unit": "chain-trajectories/s",
-                       "cg_rel_tol": 1e-12, "kernel_instance": block}
+                       "cg_rel_tol": 1e-12, "kernel_instance": block, "trajectories": batch_steps}
     out["batch"] = batch
     out["reference_host"] = cpu_c1()
     ref = out["reference_host"]["value"]
