@@ -101,7 +101,7 @@ def test_batch_mixed_sizes_many_chains(tg):
         prev = res
 
 
-@pytest.mark.parametrize("instance", [51221, 51241, 25641, 451221, 951241])
+@pytest.mark.parametrize("instance", [51221, 51241, 25641, 451221, 951241, 1451241])
 def test_cluster_instances_match_block_instance(tg, instance):
     """Chains split over thread-block clusters (2 or 4 blocks, distributed
     shared memory sums) against one block per chain: the same trajectories to
@@ -184,3 +184,27 @@ def test_solo_blocks_reproduce_one_block_instance(tg):
     for inst in (451241, 451221):
         assert out[inst] == out[51201]
         assert all(np.array_equal(a, b) for a, b in zip(out[inst, "A"], out[51201, "A"]))
+
+
+def test_pair_instance_is_reproducible(tg):
+    """Instance 1451241: 4-block clusters for the chains whose estimated cost
+    exceeds twice an SM's share, pairs of blocks (mbarrier-synchronised teams
+    inside a cluster) for the rest of the queue up to its first chain of at most
+    64^2 sites, one block from there on, with filler blocks beside.  Which team
+    runs a chain is fixed by its queue position, so two runs give bitwise the
+    same trajectories, and every chain runs."""
+    from thirring2d_gb300.workloads import mixed_size_chains
+    chains, fields = mixed_size_chains(256, seed=12)
+    out = []
+    for _ in range(2):
+        B = make_batch(tg, chains, fields)
+        bp = tg.batch_params(nsteps=6, block=1451241,
+                             cg=tg.cg_params(rel_tol=1e-10, abs_tol2=0.0, precision=1, ru_interval=50))
+        res = [B.trajectory(bp) for _ in range(2)]
+        out.append(([[(r.dH, r.accepted, r.cg_iterations, r.status) for r in t] for t in res],
+                    [B.get_gauge(i) for i in range(len(chains))]))
+        B.close()
+    assert all(r[3] == 0 for t in out[0][0] for r in t)
+    assert all(r[2] > 0 for t in out[0][0] for r in t)
+    assert out[0][0] == out[1][0]
+    assert all(np.array_equal(a, b) for a, b in zip(out[0][1], out[1][1]))

@@ -26,11 +26,13 @@ __global__ void __launch_bounds__(BS, MINB) k_batch_trajectory(const BatchChain*
 const BatchCfg kBatchCfgs[kBatchNumCfgs] = {
     {128, 8, 1, 0},    {256, 4, 1, 0},    {256, 2, 1, 0},    {256, 1, 1, 0},    {384, 1, 1, 0},
     {512, 1, 1, 0},    {512, 1, 2, 0},    {512, 1, 4, 0},    {256, 1, 4, 0},    {512, 1, 2, 4096},
-    {512, 1, 2, 9216}, {512, 1, 4, 4096}, {512, 1, 4, 9216}, {256, 1, 4, 4096}, {256, 1, 4, 9216}};
+    {512, 1, 2, 9216}, {512, 1, 4, 4096}, {512, 1, 4, 9216}, {256, 1, 4, 4096}, {256, 1, 4, 9216},
+    {512, 1, 4, 4096, 1}};
 
 // the cluster kernel of instance cfg (see batch_cluster_max)
 static int cluster_kernel_of(int cfg) {
   const BatchCfg& c = kBatchCfgs[cfg];
+  if (c.pairs) return 3;
   return c.cluster == 2 ? 0 : (c.block == 512 ? 1 : 2);
 }
 

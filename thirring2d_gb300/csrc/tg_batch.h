@@ -38,6 +38,10 @@ struct BatchTraj {
   // 1 for the filler blocks beside a cluster launch: they take chains from the
   // back of the queue, at or after solo_from only
   int from_back;
+  // 4-block cluster instances with pairs: queue positions [solo_from, pair_end)
+  // run on two blocks each (PairTeam), later ones on one (pair_end = solo_from:
+  // no pairs)
+  int pair_end;
 };
 
 // Per-chain outcome of a trajectory; `traj` is the chain's Philox trajectory
@@ -51,11 +55,14 @@ struct ChainResult {
 // kernel instances of the batched trajectory: threads per block, min blocks per
 // SM, blocks per chain (1: one block per chain; > 1: a thread-block cluster),
 // and for clusters the chain size (sites) at or below which the cluster's
-// blocks split up and run one chain each (0: never)
+// blocks split up and run one chain each (0: never).  `pairs` (4-block
+// clusters): only the chains whose estimated cost exceeds twice an SM's share
+// of the batch run on four blocks; the rest of the queue up to the first small
+// chain runs on pairs of blocks (PairTeam), the queue staying largest-first.
 struct BatchCfg {
-  int block, minb, cluster, solo_sites;
+  int block, minb, cluster, solo_sites, pairs;
 };
-constexpr int kBatchNumCfgs = 15;
+constexpr int kBatchNumCfgs = 16;
 extern const BatchCfg kBatchCfgs[kBatchNumCfgs];
 
 // The work queue is one 64-bit word (0 at launch): the low half counts the
@@ -75,12 +82,14 @@ void batch_filler_launch(cudaStream_t s, int cfg, int blocks, const BatchChain* 
 // teams (blocks or clusters) of instance cfg that can be resident at once (0: cannot launch)
 int batch_teams(int cfg, int sms);
 // the tuned instance as reported to callers: block * 100 + 10 * cluster (if > 1)
-// + min blocks per SM, + 100000 * (solo_sites / 1024)
+// + min blocks per SM, + 100000 * (solo_sites / 1024), + 1000000 with pairs
 inline int batch_cfg_id(const BatchCfg& c) {
-  return c.block * 100 + (c.cluster > 1 ? 10 * c.cluster : 0) + c.minb + 100000 * (c.solo_sites / 1024);
+  return c.block * 100 + (c.cluster > 1 ? 10 * c.cluster : 0) + c.minb + 100000 * (c.solo_sites / 1024) +
+         1000000 * c.pairs;
 }
 
-// tg_batch_cluster.cu: instance `which` (0: 512 x 2 blocks, 1: 512 x 4, 2: 256 x 4)
+// tg_batch_cluster.cu: instance `which` (0: 512 x 2 blocks, 1: 512 x 4, 2: 256 x 4,
+// 3: 512 x 4 with pairs)
 int batch_cluster_max(int which);
 void batch_cluster_launch(cudaStream_t s, int which, int clusters, const BatchChain* chains, const int* order, int n,
                           const BatchFields& F, const BatchTraj& P, ChainResult* results,

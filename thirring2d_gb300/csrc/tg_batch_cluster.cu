@@ -7,20 +7,20 @@
 
 namespace tg {
 
-template <int BS, int CL>
+template <int BS, int CL, bool PAIRS = false>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BS, 1)
     k_batch_cluster(const BatchChain* __restrict__ chains, const int* __restrict__ order, int n, BatchFields F,
                     BatchTraj P, ChainResult* results, unsigned long long* queue) {
-  batch_trajectory_body<BS, 1, ClusterTeam<CL>>(chains, order, n, F, P, results, queue);
+  batch_trajectory_body<BS, 1, ClusterTeam<CL>, PAIRS>(chains, order, n, F, P, results, queue);
 }
 
-template <int BS, int CL> int max_clusters_of() {
+template <int BS, int CL, bool PAIRS = false> int max_clusters_of() {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CL);
   cfg.blockDim = dim3(BS);
   cfg.dynamicSmemBytes = 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k_batch_cluster<BS, CL>, &cfg) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveClusters(&n, k_batch_cluster<BS, CL, PAIRS>, &cfg) != cudaSuccess) {
     cudaGetLastError();  // clear it: the instance is just not offered
     return 0;
   }
@@ -31,6 +31,7 @@ int batch_cluster_max(int which) {
   switch (which) {
     case 0: return max_clusters_of<512, 2>();
     case 1: return max_clusters_of<512, 4>();
+    case 3: return max_clusters_of<512, 4, true>();
     default: return max_clusters_of<256, 4>();
   }
 }
@@ -40,6 +41,9 @@ void batch_cluster_launch(cudaStream_t s, int which, int clusters, const BatchCh
   switch (which) {
     case 0: k_batch_cluster<512, 2><<<clusters * 2, 512, 0, s>>>(chains, order, n, F, P, results, queue); break;
     case 1: k_batch_cluster<512, 4><<<clusters * 4, 512, 0, s>>>(chains, order, n, F, P, results, queue); break;
+    case 3:
+      k_batch_cluster<512, 4, true><<<clusters * 4, 512, 0, s>>>(chains, order, n, F, P, results, queue);
+      break;
     default: k_batch_cluster<256, 4><<<clusters * 4, 256, 0, s>>>(chains, order, n, F, P, results, queue); break;
   }
 }

@@ -144,6 +144,109 @@ template <int CL> struct ClusterTeam {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Two blocks of a 4-block cluster, cluster ranks 2k and 2k + 1, running one
+// chain while the other two run another (a cluster instance's middle class of
+// chains, between the 4-block and the one-block ones).  The cluster barrier
+// would tie the two pairs together, so each block has an mbarrier of two
+// arrivals per phase: its own, and its partner's, made remotely through
+// distributed shared memory.  A block's phase k + 1 cannot complete before
+// its own arrival k + 1, which follows its wait for phase k, so the partner
+// can never run two phases ahead.  Arrivals release and the wait acquires at
+// cluster scope, ordering the blocks' global and shared memory accesses.  The
+// wait is bounded; a block that gives up counts it, the chain's result is
+// marked TG_E_TIMEOUT, and the GPU stays usable.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long* pair_mbar() {
+  __shared__ __align__(8) unsigned long long m;
+  return &m;
+}
+__device__ __forceinline__ unsigned& pair_parity() {
+  __shared__ unsigned p;
+  return p;
+}
+__device__ __forceinline__ int& pair_timeouts() {
+  __shared__ int t;
+  return t;
+}
+// at kernel start, thread 0 of every block; a cluster barrier must follow
+// before any block arrives remotely
+__device__ __forceinline__ void pair_barrier_init() {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(pair_mbar());
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(a) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  pair_parity() = 0;
+  pair_timeouts() = 0;
+}
+__device__ __forceinline__ void pair_barrier() {
+  __syncthreads();  // the block's writes before thread 0's arrival
+  if (threadIdx.x == 0) {
+    const unsigned own = (unsigned)__cvta_generic_to_shared(pair_mbar());
+    const unsigned partner = cooperative_groups::this_cluster().block_rank() ^ 1u;
+    unsigned remote;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(own), "r"(partner));
+    unsigned long long state;
+    asm volatile("mbarrier.arrive.release.cluster.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(own) : "memory");
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(remote) : "memory");
+    const unsigned parity = pair_parity();
+    unsigned done = 0;
+    for (int i = 0; i < (1 << 20) && !done; i++) {  // each try may suspend the thread briefly
+      asm volatile(
+          "{\n\t.reg .pred p;\n\t"
+          "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+          "selp.u32 %0, 1, 0, p;\n\t}"
+          : "=r"(done)
+          : "r"(own), "r"(parity)
+          : "memory");
+    }
+    if (!done) pair_timeouts() += 1;
+    pair_parity() = parity ^ 1u;
+    (void)state;
+  }
+  __syncthreads();
+}
+
+struct PairTeam {
+  __device__ static int rank() { return (int)(cooperative_groups::this_cluster().block_rank() & 1u); }
+  __device__ static int nblocks() { return 2; }
+  __device__ static void sync() { pair_barrier(); }
+  template <typename P, class F> __device__ static auto sum_then(P v, F f) -> decltype(f(0.0)) {
+    using S = decltype(f(0.0));
+    static_assert(sizeof(S) <= sizeof(TeamScratch::out), "sum_then result too large");
+    TeamScratch& sc = team_scratch();
+    const double b = block_total_warp0(v, sc);
+    int ph = 0;
+    if (threadIdx.x == 0) {
+      ph = sc.phase;
+      sc.total[ph] = b;
+    }
+    pair_barrier();  // both totals written
+    if (threadIdx.x == 0) {
+      cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+      const double mine = sc.total[ph];
+      const double other = cl.map_shared_rank(sc.total, cl.block_rank() ^ 1u)[ph];
+      const double s = (rank() == 0) ? mine + other : other + mine;  // pair rank 0's total first
+      *reinterpret_cast<S*>(sc.out) = f(s);
+      sc.phase = ph ^ 1;
+    }
+    // as in ClusterTeam: the slot just read is written again two sums later,
+    // after the next sum's pair barrier
+    __syncthreads();
+    return *reinterpret_cast<const S*>(sc.out);
+  }
+  static constexpr bool kCluster = false;
+  __device__ static void init() {}
+  __device__ static double sum(double v) { return sum_then(v, [](double t) { return t; }); }
+  // the ticket pair rank 0's thread 0 wrote to `next`
+  __device__ static int broadcast(const int* next) {
+    pair_barrier();
+    cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+    const int q = (rank() == 0) ? *next : *cl.map_shared_rank(next, cl.block_rank() ^ 1u);
+    pair_barrier();
+    return q;
+  }
+};
+
 // the chain's sites, split over the whole team
 #define TG_BSITES(s, n) \
   for (int s = T::rank() * (int)blockDim.x + (int)threadIdx.x; s < (n); s += T::nblocks() * (int)blockDim.x)
@@ -537,7 +640,7 @@ __device__ __forceinline__ int queue_back(unsigned long long* queue, int n, int 
   return n;
 }
 
-template <int BS, int MINB, class T>
+template <int BS, int MINB, class T, bool PAIRS = false>
 __device__ __forceinline__ void batch_trajectory_body(const BatchChain* __restrict__ chains,
                                                       const int* __restrict__ order, int n, const BatchFields& F,
                                                       const BatchTraj& P, ChainResult* results,
@@ -547,6 +650,9 @@ __device__ __forceinline__ void batch_trajectory_body(const BatchChain* __restri
   // block of a team fills its own copy.
   __shared__ int next;
   __shared__ ChainCtx c;
+  if constexpr (PAIRS) {
+    if (threadIdx.x == 0) pair_barrier_init();
+  }
   T::init();  // published by the first broadcast's barriers
   int q;
   while (true) {
@@ -561,11 +667,46 @@ __device__ __forceinline__ void batch_trajectory_body(const BatchChain* __restri
     else chain_trajectory<false, T>(c, P, &results[ci]);
   }
   if constexpr (T::kCluster) {
+    int carry = -1;  // a ticket past pair_end that this block runs alone
+    if constexpr (PAIRS) {
+      // Queue positions [solo_from, pair_end): the cluster splits into two
+      // pairs; ranks 0-1 run chain q, ranks 2-3 take the next.  A pair whose
+      // ticket lies past pair_end splits again: its rank 0 runs that chain
+      // alone.  (The broadcast's closing cluster barrier has ordered every
+      // earlier access; each pair's blocks touch only each other's shared
+      // memory.)
+      if (q < n && q < P.pair_end) {
+        const bool first = (cooperative_groups::this_cluster().block_rank() >> 1) == 0;
+        int pq = first ? q : -1;
+        while (true) {
+          if (pq < 0) {
+            if (PairTeam::rank() == 0 && threadIdx.x == 0) next = queue_front(queue, n);
+            pq = PairTeam::broadcast(&next);
+          }
+          if (pq >= n) break;
+          if (pq >= P.pair_end) {
+            if (PairTeam::rank() == 0) carry = pq;
+            break;
+          }
+          const int ci = order[pq];
+          if (threadIdx.x == 0) {
+            fill_ctx(c, chains[ci], F);
+            pair_timeouts() = 0;
+          }
+          __syncthreads();
+          if (c.mu == 0.0) chain_trajectory<true, PairTeam>(c, P, &results[ci]);
+          else chain_trajectory<false, PairTeam>(c, P, &results[ci]);
+          if (PairTeam::rank() == 0 && threadIdx.x == 0 && pair_timeouts() > 0) results[ci].status = TG_E_TIMEOUT;
+          pq = -1;
+        }
+        q = n;  // q was run by a pair
+      }
+    }
     // The rest of the queue holds small chains: rank 0 runs chain q and every
     // block then takes chains of its own, with block barriers only.  No block
     // touches another's shared memory from here on (the broadcast's closing
     // cluster barrier has ordered every earlier access).
-    int mine = (q < n && T::rank() == 0) ? q : -1;
+    int mine = (q < n && T::rank() == 0) ? q : carry;
     while (true) {
       if (mine < 0) {
         if (threadIdx.x == 0) next = queue_front(queue, n);

@@ -1492,6 +1492,9 @@ struct tg_batch {
   cudaStream_t stream = nullptr;
   cudaStream_t filler = nullptr;               // the filler blocks' stream (batch_filler_launch)
   cudaEvent_t fork = nullptr, join = nullptr;  // ordering it into `stream` (also under graph capture)
+  // instances with pairs: the queue's first pair_top chains (estimated cost
+  // above twice an SM's share of the batch) run on 4-block clusters
+  int pair_top = 0;
   BatchChain* d_chains = nullptr;
   int* d_order = nullptr;
   ChainResult* d_res = nullptr;
@@ -1535,17 +1538,21 @@ int batch_launch(tg_batch* B, const tg_batch_params& p, int cfg, cudaStream_t s)
         t.solo_from = q;
         break;
       }
+  t.pair_end = t.solo_from;
+  if (kBatchCfgs[cfg].pairs) t.solo_from = std::min(B->pair_top, t.pair_end);
   TG_CK(cudaMemsetAsync(B->d_queue, 0, sizeof(unsigned long long), s));
   // filler blocks on the SMs the clusters leave idle, on a stream forked from s
   // after the queue's reset and joined back into s; launched after the cluster
   // kernel, whose clusters should take their SMs first
-  const int fill = (t.solo_from < B->n) ? batch_filler_blocks(cfg, B->sms) : 0;
+  const int fill = (t.pair_end < B->n) ? batch_filler_blocks(cfg, B->sms) : 0;
   if (fill > 0) TG_CK(cudaEventRecord(B->fork, s));
   batch_trajectory(s, cfg, B->sms, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
   TG_CK(cudaGetLastError());
   if (fill > 0) {
+    BatchTraj tf = t;
+    tf.solo_from = t.pair_end;  // the filler draws one-block chains only
     TG_CK(cudaStreamWaitEvent(B->filler, B->fork, 0));
-    batch_filler_launch(B->filler, cfg, fill, B->d_chains, B->d_order, B->n, B->F, t, B->d_res, B->d_queue);
+    batch_filler_launch(B->filler, cfg, fill, B->d_chains, B->d_order, B->n, B->F, tf, B->d_res, B->d_queue);
     TG_CK(cudaGetLastError());
     TG_CK(cudaEventRecord(B->join, B->filler));
     TG_CK(cudaStreamWaitEvent(s, B->join, 0));
@@ -1666,6 +1673,15 @@ int tg_batch_create(const tg_chain_params* chains, int nchains, int device, tg_b
   if (cudaMallocHost((void**)&B->h_res, sizeof(ChainResult) * nchains) != cudaSuccess)
     return bail(fail(TG_E_ALLOC, "pinned allocation failed"));
   B->order = order;
+  {
+    auto cost = [&](int c) { return (double)hc[c].geo.V / std::max(fabs(hc[c].m), 1e-3); };
+    double w = 0;
+    for (int c = 0; c < nchains; c++) w += cost(c);
+    const double share = w / B->sms;
+    int top = 0;
+    while (top < nchains && cost(order[top]) > 2.0 * share) top++;
+    B->pair_top = top;
+  }
   if (cudaMemcpyAsync(B->d_chains, hc.data(), sizeof(BatchChain) * nchains, cudaMemcpyHostToDevice, B->stream) !=
           cudaSuccess ||
       cudaMemcpyAsync(B->d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, B->stream) !=
