@@ -607,11 +607,14 @@ __device__ __forceinline__ float4 axpy4(float a, float4 x, float4 y) {
   return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
 }
 
-// Phase A over two sites per float4, two float4 per thread in flight.
+// Phase A over two sites per float4, one float4 per thread and array in flight
+// (U = 1: the kernel then needs no local memory at all; U = 2 spilled 32-48 B
+// and was 0.9% slower per iteration at 2048^2, U = 3 spilled 112 B and was 7%
+// slower).
 __device__ __forceinline__ void cgcg_update(const Geo& g, float4* __restrict__ r, const float4* __restrict__ w,
                                             float4* __restrict__ s, float4* __restrict__ p, float4* __restrict__ xs,
                                             float al, float be) {
-  constexpr int U = 2;
+  constexpr int U = 1;
   const int n4 = g.V >> 1;  // V is even on column-march lattices
   const int stride = gridDim.x * blockDim.x;
   for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n4; i0 += U * stride) {
